@@ -1,0 +1,430 @@
+// C ABI of the engine (include/gbt_tsdf.h): volume lifetime, argument
+// checking, pose conversion and kernel dispatch.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "gbt_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gbt_status fail(gbt_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+gbt_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(GBT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int device_sms() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+}  // namespace
+
+struct gbt_volume {
+    gbt_volume_cfg cfg;
+    gbt::VolDesc desc;
+    int64_t nvox;
+    bool managed;
+    void* tvox;
+    // marching-cubes scratch: [0,64) header (ticket u32, error i32, total i64), then status words
+    void* mc_scratch;
+    size_t mc_scratch_bytes;
+};
+
+namespace gbt {
+
+int integrate_default_ctas_per_sm() { return 8; }
+
+void brick_extent(int brick, int* bx, int* by, int* bz) {
+    switch (brick) {
+        case 1: *bx = 16; *by = 8; *bz = 4; break;
+        case 2: *bx = 32; *by = 2; *bz = 8; break;
+        case 3: *bx = 64; *by = 2; *bz = 4; break;
+        default: *bx = 32; *by = 4; *bz = 4; break;
+    }
+}
+
+}  // namespace gbt
+
+namespace {
+
+// Fixed-mode projection K [R | t] from the pose, in double, rounded once to
+// float.  The quaternion is normalised first.
+void fixed_projection(const double* pose, const gbt_volume_cfg& c, float* P) {
+    double qw = pose[0], qx = pose[1], qy = pose[2], qz = pose[3];
+    const double n = std::sqrt(qw * qw + qx * qx + qy * qy + qz * qz);
+    qw /= n;
+    qx /= n;
+    qy /= n;
+    qz /= n;
+    double R[9];
+    R[0] = 1 - 2 * (qy * qy + qz * qz);
+    R[1] = 2 * (qx * qy - qz * qw);
+    R[2] = 2 * (qx * qz + qy * qw);
+    R[3] = 2 * (qx * qy + qz * qw);
+    R[4] = 1 - 2 * (qx * qx + qz * qz);
+    R[5] = 2 * (qy * qz - qx * qw);
+    R[6] = 2 * (qx * qz - qy * qw);
+    R[7] = 2 * (qy * qz + qx * qw);
+    R[8] = 1 - 2 * (qx * qx + qy * qy);
+    const double t[3] = {pose[4], pose[5], pose[6]};
+    const double fx = c.focal_x, fy = c.focal_y, cx = c.cx, cy = c.cy;
+    for (int k = 0; k < 3; ++k) {
+        P[0 + k] = (float)(fx * R[0 + k] + cx * R[6 + k]);
+        P[4 + k] = (float)(fy * R[3 + k] + cy * R[6 + k]);
+        P[8 + k] = (float)R[6 + k];
+    }
+    P[3] = (float)(fx * t[0] + cx * t[2]);
+    P[7] = (float)(fy * t[1] + cy * t[2]);
+    P[11] = (float)t[2];
+}
+
+gbt_status check_frames(const gbt_frame* frames, int32_t nframes) {
+    if (!frames) return fail(GBT_ERR_INVALID_ARG, "frames is NULL");
+    if (nframes < 1 || nframes > GBT_MAX_FRAMES_PER_PASS)
+        return fail(GBT_ERR_INVALID_ARG, "nframes %d outside 1..%d", nframes, GBT_MAX_FRAMES_PER_PASS);
+    for (int i = 0; i < nframes; ++i) {
+        const gbt_frame& f = frames[i];
+        // tsdf_volume.cu:260-268
+        if (!f.depth) return fail(GBT_ERR_INVALID_ARG, "frame %d: depth map is a null pointer", i);
+        if (f.width <= 0 || f.height <= 0)
+            return fail(GBT_ERR_INVALID_ARG, "frame %d: depth width/height are zero", i);
+        if (f.format != GBT_DEPTH_F32_M && f.format != GBT_DEPTH_U16)
+            return fail(GBT_ERR_INVALID_ARG, "frame %d: unknown depth format %d", i, f.format);
+        const size_t elem = f.format == GBT_DEPTH_U16 ? 2 : 4;
+        if (f.pitch_bytes < elem * (size_t)f.width)
+            return fail(GBT_ERR_INVALID_ARG, "frame %d: pitch %zu below width*%zu", i, f.pitch_bytes, elem);
+        if (f.pitch_bytes % elem != 0 || ((uintptr_t)f.depth % elem) != 0)
+            return fail(GBT_ERR_INVALID_ARG, "frame %d: depth rows not aligned to the element size", i);
+        for (int k = 0; k < 7; ++k)
+            if (!std::isfinite(f.pose[k])) return fail(GBT_ERR_INVALID_ARG, "frame %d: pose is not finite", i);
+    }
+    return GBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbt_last_error(void) { return g_last_error.c_str(); }
+
+const char* gbt_version(void) { return "gbt-tsdf 0.1 sm_103a"; }
+
+gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume** out) {
+    if (!cfg || !out) return fail(GBT_ERR_INVALID_ARG, "cfg or out is NULL");
+    *out = nullptr;
+    const gbt_volume_cfg& c = *cfg;
+    for (int i = 0; i < 3; ++i) {
+        if (c.voxel_grid_size[i] == 0) return fail(GBT_ERR_INVALID_ARG, "voxel_grid_size[%d] is 0", i);
+        if (!(c.physical_size[i] > 0.f) || !std::isfinite(c.physical_size[i]))
+            return fail(GBT_ERR_INVALID_ARG, "physical_size[%d] must be positive", i);
+        if (!std::isfinite(c.global_offset[i])) return fail(GBT_ERR_INVALID_ARG, "global_offset[%d] not finite", i);
+        if (c.voxel_grid_size[i] > (1u << 24))
+            return fail(GBT_ERR_INVALID_ARG, "voxel_grid_size[%d] above 2^24", i);
+    }
+    const int64_t nvox = (int64_t)c.voxel_grid_size[0] * c.voxel_grid_size[1] * c.voxel_grid_size[2];
+    if (nvox >= (int64_t)1 << 32) return fail(GBT_ERR_INVALID_ARG, "volume has %lld voxels; limit is 2^32-1", (long long)nvox);
+    if (c.mode != GBT_MODE_COMPAT && c.mode != GBT_MODE_FIXED) return fail(GBT_ERR_INVALID_ARG, "unknown mode %d", c.mode);
+    if (c.arith != GBT_ARITH_REFERENCE && c.arith != GBT_ARITH_IEEE)
+        return fail(GBT_ERR_INVALID_ARG, "unknown arith %d", c.arith);
+    if (c.memory != GBT_MEMORY_DEVICE && c.memory != GBT_MEMORY_MANAGED)
+        return fail(GBT_ERR_INVALID_ARG, "unknown memory kind %d", c.memory);
+    if (c.mode == GBT_MODE_FIXED && !(c.max_weight >= 1.f))
+        return fail(GBT_ERR_INVALID_ARG, "fixed mode needs max_weight >= 1");
+    if (!std::isfinite(c.focal_x) || !std::isfinite(c.focal_y) || !std::isfinite(c.cx) || !std::isfinite(c.cy))
+        return fail(GBT_ERR_INVALID_ARG, "intrinsics not finite");
+
+    gbt_volume* v = new gbt_volume();
+    std::memset(v, 0, sizeof(*v));
+    v->cfg = c;
+    v->nvox = nvox;
+    v->managed = c.memory == GBT_MEMORY_MANAGED;
+    gbt::VolDesc& d = v->desc;
+    d.nx = (int32_t)c.voxel_grid_size[0];
+    d.ny = (int32_t)c.voxel_grid_size[1];
+    d.nz = (int32_t)c.voxel_grid_size[2];
+    // tsdf_volume.cu:197-199
+    for (int i = 0; i < 3; ++i) {
+        d.vs[i] = c.physical_size[i] / (float)c.voxel_grid_size[i];
+        d.off[i] = c.global_offset[i];
+    }
+    float dot = d.vs[0] * d.vs[0] + d.vs[1] * d.vs[1];
+    dot = dot + d.vs[2] * d.vs[2];
+    d.trunc = c.truncation > 0.f ? c.truncation : 1.1f * std::sqrt(dot);
+    d.max_weight = c.max_weight;
+    d.max_depth = c.max_depth > 0.f ? c.max_depth : 24.0f;
+    d.min_z = c.min_z;
+    d.fx = c.focal_x;
+    d.fy = c.focal_y;
+    d.cx = c.cx;
+    d.cy = c.cy;
+
+    const size_t bytes = (size_t)nvox * sizeof(float);
+    cudaError_t e;
+    if (v->managed) {
+        e = cudaMallocManaged(&d.D, bytes, cudaMemAttachGlobal);
+        if (e == cudaSuccess) e = cudaMallocManaged(&d.W, bytes, cudaMemAttachGlobal);
+    } else {
+        e = cudaMalloc(&d.D, bytes);
+        if (e == cudaSuccess) e = cudaMalloc(&d.W, bytes);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (d.D) cudaFree(d.D);
+        if (d.W) cudaFree(d.W);
+        delete v;
+        return fail(GBT_ERR_ALLOC, "allocating %zu bytes for the volume: %s", 2 * bytes, cudaGetErrorString(e));
+    }
+    gbt_status st = gbt_volume_reset(v, stream);
+    if (st == GBT_OK) {
+        e = cudaStreamSynchronize(as_stream(stream));
+        if (e != cudaSuccess) st = cuda_fail(e, "volume set-up");
+    }
+    if (st != GBT_OK) {
+        cudaFree(d.D);
+        cudaFree(d.W);
+        delete v;
+        return st;
+    }
+    *out = v;
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_destroy(gbt_volume* v) {
+    if (!v) return GBT_OK;
+    cudaFree(v->desc.D);
+    cudaFree(v->desc.W);
+    if (v->tvox) cudaFree(v->tvox);
+    if (v->mc_scratch) cudaFree(v->mc_scratch);
+    delete v;
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_reset(gbt_volume* v, void* stream) {
+    if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    cudaError_t e = gbt::launch_volume_init(v->desc.D, v->desc.W, v->nvox, v->desc.trunc, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "volume initialisation");
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_get_info(const gbt_volume* v, gbt_volume_info* info) {
+    if (!v || !info) return fail(GBT_ERR_INVALID_ARG, "volume or info is NULL");
+    std::memset(info, 0, sizeof(*info));
+    for (int i = 0; i < 3; ++i) {
+        info->voxel_grid_size[i] = v->cfg.voxel_grid_size[i];
+        info->voxel_size[i] = v->desc.vs[i];
+        info->global_offset[i] = v->cfg.global_offset[i];
+        info->physical_size[i] = v->cfg.physical_size[i];
+    }
+    info->truncation = v->desc.trunc;
+    info->num_voxels = v->nvox;
+    info->tsdf = v->desc.D;
+    info->weights = v->desc.W;
+    info->mode = v->cfg.mode;
+    info->arith = v->cfg.arith;
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_transformation_voxels(gbt_volume* v, void* stream, void** out) {
+    if (!v || !out) return fail(GBT_ERR_INVALID_ARG, "volume or out is NULL");
+    if (!v->tvox) {
+        const size_t bytes = (size_t)v->nvox * 28;
+        cudaError_t e = v->managed ? cudaMallocManaged(&v->tvox, bytes, cudaMemAttachGlobal) : cudaMalloc(&v->tvox, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            v->tvox = nullptr;
+            return fail(GBT_ERR_ALLOC, "allocating %zu bytes of voxel transforms: %s", bytes, cudaGetErrorString(e));
+        }
+        e = gbt::launch_tvoxels(v->tvox, v->desc, as_stream(stream));
+        if (e != cudaSuccess) return cuda_fail(e, "voxel transforms");
+    }
+    *out = v->tvox;
+    return GBT_OK;
+}
+
+gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t nframes, int32_t brick,
+                               int32_t ctas_per_sm, void* stream) {
+    if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    gbt_status st = check_frames(frames, nframes);
+    if (st != GBT_OK) return st;
+    if (brick < 0 || brick > 3) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..3", brick);
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(GBT_ERR_INVALID_ARG, "ctas_per_sm %d outside 0..32", ctas_per_sm);
+    gbt::IntegrateArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.vol = v->desc;
+    a.nframes = nframes;
+    for (int i = 0; i < nframes; ++i) {
+        const gbt_frame& f = frames[i];
+        gbt::FrameDesc& fd = a.frames[i];
+        fd.depth = f.depth;
+        fd.pitch = (int64_t)f.pitch_bytes;
+        fd.width = f.width;
+        fd.height = f.height;
+        fd.fmt = f.format;
+        fd.scale = f.depth_scale;
+        // tsdf_volume.cu:271-272
+        fd.q[0] = (float)f.pose[1];
+        fd.q[1] = (float)f.pose[2];
+        fd.q[2] = (float)f.pose[3];
+        fd.q[3] = (float)f.pose[0];
+        fd.t[0] = (float)f.pose[4];
+        fd.t[1] = (float)f.pose[5];
+        fd.t[2] = (float)f.pose[6];
+        if (v->cfg.mode == GBT_MODE_FIXED) fixed_projection(f.pose, v->cfg, fd.P);
+        if (v->cfg.mode == GBT_MODE_COMPAT && f.format != GBT_DEPTH_F32_M)
+            return fail(GBT_ERR_INVALID_ARG, "compat mode takes float depth in metres (frame %d)", i);
+    }
+    int bx, by, bz;
+    gbt::brick_extent(brick, &bx, &by, &bz);
+    const long long nbricks = (long long)((v->desc.nx + bx - 1) / bx) * ((v->desc.ny + by - 1) / by) *
+                              ((v->desc.nz + bz - 1) / bz);
+    long long grid = (long long)device_sms() * (ctas_per_sm ? ctas_per_sm : gbt::integrate_default_ctas_per_sm());
+    if (grid > nbricks) grid = nbricks;
+    if (grid < 1) grid = 1;
+    cudaError_t e;
+    if (v->cfg.mode == GBT_MODE_FIXED)
+        e = gbt::launch_integrate_fixed(a, brick, (int)grid, as_stream(stream));
+    else if (v->cfg.arith == GBT_ARITH_IEEE)
+        e = gbt::launch_integrate_compat_ieee(a, brick, (int)grid, as_stream(stream));
+    else
+        e = gbt::launch_integrate_compat_ref(a, brick, (int)grid, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "integrate launch");
+    return GBT_OK;
+}
+
+gbt_status gbt_integrate(gbt_volume* v, const gbt_frame* frames, int32_t nframes, void* stream) {
+    return gbt_integrate_tuned(v, frames, nframes, 0, 0, stream);
+}
+
+}  // extern "C"
+
+namespace {
+
+gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, int64_t index_base, gbt::McArgs* a) {
+    if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    if (cap < 0) return fail(GBT_ERR_INVALID_ARG, "negative capacity");
+    if (cap > 0 && (!verts || !tris)) return fail(GBT_ERR_INVALID_ARG, "output buffers are NULL");
+    const gbt::VolDesc& d = v->desc;
+    std::memset(a, 0, sizeof(*a));
+    a->D = d.D;
+    a->W = d.W;
+    a->gx = d.nx;
+    a->gy = d.ny;
+    a->gz = d.nz;
+    for (int i = 0; i < 3; ++i) {
+        a->vs[i] = d.vs[i];
+        a->off[i] = d.off[i];
+    }
+    const int64_t ncubes = (d.nx >= 2 && d.ny >= 2 && d.nz >= 2)
+                               ? (int64_t)(d.nx - 1) * (d.ny - 1) * (d.nz - 1) : 0;
+    a->ncubes = (uint32_t)ncubes;
+    a->ntiles = (uint32_t)((ncubes + gbt::kMcTile - 1) / gbt::kMcTile);
+    a->div_cx = gbt::make_fastdiv((uint32_t)(d.nx > 1 ? d.nx - 1 : 1));
+    a->div_cy = gbt::make_fastdiv((uint32_t)(d.ny > 1 ? d.ny - 1 : 1));
+    a->div_gx = gbt::make_fastdiv((uint32_t)d.nx);
+    a->div_gy = gbt::make_fastdiv((uint32_t)d.ny);
+    a->verts = verts;
+    a->tris = tris;
+    a->cap = cap;
+    a->index_base = index_base;
+    const size_t need = 64 + (size_t)a->ntiles * 8;
+    if (v->mc_scratch_bytes < need) {
+        if (v->mc_scratch) cudaFree(v->mc_scratch);
+        v->mc_scratch = nullptr;
+        v->mc_scratch_bytes = 0;
+        cudaError_t e = cudaMalloc(&v->mc_scratch, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GBT_ERR_ALLOC, "allocating %zu bytes of mesh scratch: %s", need, cudaGetErrorString(e));
+        }
+        v->mc_scratch_bytes = need;
+    }
+    char* s = static_cast<char*>(v->mc_scratch);
+    a->ticket = reinterpret_cast<unsigned int*>(s);
+    a->error = reinterpret_cast<int*>(s + 4);
+    a->total = reinterpret_cast<long long*>(s + 8);
+    a->status = reinterpret_cast<unsigned long long*>(s + 64);
+    return GBT_OK;
+}
+
+gbt_status mc_launch(gbt_volume* v, const gbt::McArgs& a, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(v->mc_scratch, 0, 64 + (size_t)a.ntiles * 8, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh scratch clear");
+    if (a.ntiles == 0) return GBT_OK;
+    if (v->cfg.mode == GBT_MODE_FIXED)
+        e = gbt::launch_mc_fixed(a, s);
+    else if (v->cfg.arith == GBT_ARITH_IEEE)
+        e = gbt::launch_mc_compat_ieee(a, s);
+    else
+        e = gbt::launch_mc_compat_ref(a, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh launch");
+    return GBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbt_status gbt_extract_mesh(gbt_volume* v, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
+                            int64_t* n_tris, void* stream) {
+    if (!n_tris) return fail(GBT_ERR_INVALID_ARG, "n_tris is NULL");
+    *n_tris = 0;
+    gbt::McArgs a;
+    gbt_status st = mc_prepare(v, verts, tris, cap_tris, index_base, &a);
+    if (st != GBT_OK) return st;
+    cudaStream_t s = as_stream(stream);
+    st = mc_launch(v, a, s);
+    if (st != GBT_OK) return st;
+    struct {
+        unsigned int ticket;
+        int error;
+        long long total;
+    } hdr;
+    cudaError_t e = cudaMemcpyAsync(&hdr, v->mc_scratch, sizeof(hdr), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh extraction");
+    if (hdr.error) return fail(GBT_ERR_TIMEOUT, "mesh extraction: a tile gave up waiting for its predecessor");
+    *n_tris = hdr.total;
+    if (hdr.total > cap_tris && cap_tris > 0)
+        return fail(GBT_ERR_CAPACITY, "mesh has %lld triangles, buffer holds %lld", hdr.total, (long long)cap_tris);
+    return GBT_OK;
+}
+
+gbt_status gbt_extract_mesh_async(gbt_volume* v, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
+                                  int64_t* d_n_tris, void* stream) {
+    if (!d_n_tris) return fail(GBT_ERR_INVALID_ARG, "d_n_tris is NULL");
+    gbt::McArgs a;
+    gbt_status st = mc_prepare(v, verts, tris, cap_tris, index_base, &a);
+    if (st != GBT_OK) return st;
+    cudaStream_t s = as_stream(stream);
+    st = mc_launch(v, a, s);
+    if (st != GBT_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(d_n_tris, a.total, sizeof(long long), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh count copy");
+    return GBT_OK;
+}
+
+}  // extern "C"

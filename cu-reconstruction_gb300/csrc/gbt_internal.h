@@ -1,0 +1,112 @@
+// Types shared by the engine's translation units: the kernel argument blocks
+// and the host-side launchers each kernel TU exports.  Not part of the ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gbt_tsdf.h"
+
+namespace gbt {
+
+// Volume as the kernels see it.  D and W are [nz][ny][nx], x fastest.
+struct VolDesc {
+    float* D;
+    float* W;
+    int32_t nx, ny, nz;
+    int32_t pad0;
+    float vs[3];
+    float off[3];
+    float trunc;
+    float max_weight;
+    float max_depth;
+    float min_z;
+    float fx, fy, cx, cy;
+};
+
+// One frame as the kernels see it.  q/t: the reference's float quaternion
+// (x, y, z, w) and translation; P: rows of K[R|t] for the fixed mode.
+struct FrameDesc {
+    const void* depth;
+    int64_t pitch;
+    int32_t width, height;
+    int32_t fmt;
+    float scale;
+    float q[4];
+    float t[3];
+    float P[12];
+};
+
+struct IntegrateArgs {
+    VolDesc vol;
+    int32_t nframes;
+    int32_t pad0;
+    FrameDesc frames[GBT_MAX_FRAMES_PER_PASS];
+};
+
+// Unsigned 32-bit division by a run-time invariant divisor with one
+// multiply-high, after Granlund & Montgomery, "Division by invariant integers
+// using multiplication" (PLDI 1994), figure 4.1.
+struct FastDiv {
+    uint32_t d;
+    uint32_t m;
+    uint32_t s;
+    uint32_t pad0;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f{d, 0u, 0u, 0u};
+    if (d <= 1) return f;
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    f.s = l;
+    return f;
+}
+
+// Marching cubes over the linear cube order (z, y, x), one tile of
+// kMcTile cubes per CTA, tiles chained by a decoupled look-back.
+constexpr int kMcThreads = 256;
+constexpr int kMcCubesPerThread = 4;
+constexpr int kMcTile = kMcThreads * kMcCubesPerThread;
+
+struct McArgs {
+    const float* D;
+    const float* W;
+    int32_t gx, gy, gz;
+    int32_t pad0;
+    float vs[3];
+    float off[3];
+    FastDiv div_cx;   // gx - 1
+    FastDiv div_cy;   // gy - 1
+    FastDiv div_gx;   // gx
+    FastDiv div_gy;   // gy
+    uint32_t ncubes;
+    uint32_t ntiles;
+    float* verts;
+    int32_t* tris;
+    int64_t cap;
+    int64_t index_base;
+    unsigned long long* status;  // [ntiles] look-back words, zeroed before launch
+    unsigned int* ticket;        // tile ticket, zeroed before launch
+    long long* total;            // triangle count out
+    int* error;                  // set to 1 when a look-back wait gives up
+};
+
+// Launchers exported by the kernel translation units.
+// k_ref.cu (-use_fast_math): compat mode in the reference's arithmetic.
+cudaError_t launch_integrate_compat_ref(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
+cudaError_t launch_mc_compat_ref(const McArgs& a, cudaStream_t s);
+// k_ieee.cu (IEEE arithmetic): compat mode as the oracle computes it, fixed mode.
+cudaError_t launch_integrate_compat_ieee(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
+cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
+cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s);
+cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s);
+// k_util.cu: volume initialisation and the packed per-voxel transform records.
+cudaError_t launch_volume_init(float* D, float* W, int64_t n, float trunc, cudaStream_t s);
+cudaError_t launch_tvoxels(void* out, const VolDesc& v, cudaStream_t s);
+
+// CTAs per SM the integrate launchers use by default, and brick extents.
+int integrate_default_ctas_per_sm();
+void brick_extent(int brick, int* bx, int* by, int* bz);
+
+}  // namespace gbt

@@ -1,0 +1,605 @@
+// TSDF integrate and marching-cubes kernels.
+//
+// This header is compiled twice:
+//   k_ref.cu   with -use_fast_math and GBT_REF_ARITH defined: the compat mode
+//              with the reference's own arithmetic (its divisions are the
+//              approximate divide nvcc emits under fast math, its multiply-adds
+//              are contracted by the compiler exactly where the reference's are);
+//   k_ieee.cu  without fast math: every operation is an explicit IEEE
+//              intrinsic, in the order the CPU oracle uses (compat mode), plus
+//              the fixed mode.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gbt_internal.h"
+
+#define GBT_MC_CONST static __constant__
+#include "mc_tables.inc"
+GBT_MC_TABLE_DATA
+#undef GBT_MC_CONST
+
+namespace gbt {
+
+enum { kCompat = 0, kFixed = 1 };
+
+// ---------------------------------------------------------------------------
+// Arithmetic of the compat mode.  The expressions below follow the reference
+// operation for operation (se3.cuh:125-140,165-175,207-223; camera_util.cu:15-16;
+// tsdf_volume.cu:117-119,183; marching_cubes.cu:43-48) because the compat mode
+// must reproduce its results bit for bit.
+#if defined(GBT_REF_ARITH)
+
+__device__ __forceinline__ float centre(int v, float vs, float off) { return ((float)v + 0.5f) * vs + off; }
+
+__device__ __forceinline__ void compat_rotation(const float* q, float* R) {
+    const float x = 2 * q[0], y = 2 * q[1], z = 2 * q[2];
+    const float wx = x * q[3], wy = y * q[3], wz = z * q[3];
+    const float xx = x * q[0], xy = y * q[0], xz = z * q[0];
+    const float yy = y * q[1], yz = z * q[1], zz = z * q[2];
+    R[0] = 1 - (yy + zz);
+    R[1] = xy - wz;
+    R[2] = xz + wy;
+    R[3] = xy + wz;
+    R[4] = 1 - (xx + zz);
+    R[5] = yz - wx;
+    R[6] = xz - wy;
+    R[7] = yz + wx;
+    R[8] = 1 - (xx + yy);
+}
+__device__ __forceinline__ float compat_cam(float r0, float r1, float r2, float t, float px, float py, float pz) {
+    return (r0 * px + r1 * py + r2 * pz) + t;
+}
+__device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) { return (c * f) / cz + cc; }
+__device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
+    return ((d * w) + (tsdf * 1.0f)) / nw;
+}
+__device__ __forceinline__ float mc_ratio(float s, float e) { return (-s) / (e - s); }
+__device__ __forceinline__ float mc_lerp(float a, float b, float r) { return a + r * (b - a); }
+
+#else
+
+__device__ __forceinline__ float centre(int v, float vs, float off) {
+    return __fmaf_rn(__fadd_rn((float)v, 0.5f), vs, off);
+}
+__device__ __forceinline__ void compat_rotation(const float* q, float* R) {
+    const float x = __fmul_rn(2.f, q[0]), y = __fmul_rn(2.f, q[1]), z = __fmul_rn(2.f, q[2]);
+    const float wx = __fmul_rn(x, q[3]), wy = __fmul_rn(y, q[3]), wz = __fmul_rn(z, q[3]);
+    const float xx = __fmul_rn(x, q[0]), yy = __fmul_rn(y, q[1]), zz = __fmul_rn(z, q[2]);
+    R[0] = __fsub_rn(1.f, __fmaf_rn(y, q[1], zz));
+    R[1] = __fmaf_rn(y, q[0], -wz);
+    R[2] = __fmaf_rn(z, q[0], wy);
+    R[3] = __fmaf_rn(y, q[0], wz);
+    R[4] = __fsub_rn(1.f, __fmaf_rn(x, q[0], zz));
+    R[5] = __fmaf_rn(z, q[1], -wx);
+    R[6] = __fmaf_rn(z, q[0], -wy);
+    R[7] = __fmaf_rn(z, q[1], wx);
+    R[8] = __fsub_rn(1.f, __fmaf_rn(x, q[0], yy));
+}
+__device__ __forceinline__ float compat_cam(float r0, float r1, float r2, float t, float px, float py, float pz) {
+    return __fadd_rn(__fmaf_rn(r2, pz, __fmaf_rn(r0, px, __fmul_rn(r1, py))), t);
+}
+__device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) {
+    return __fadd_rn(__fdiv_rn(__fmul_rn(c, f), cz), cc);
+}
+__device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
+    return __fdiv_rn(__fmaf_rn(d, w, tsdf), nw);
+}
+__device__ __forceinline__ float mc_ratio(float s, float e) { return __fdiv_rn(-s, __fsub_rn(e, s)); }
+__device__ __forceinline__ float mc_lerp(float a, float b, float r) { return __fmaf_rn(r, __fsub_rn(b, a), a); }
+
+#endif
+
+__device__ __forceinline__ uint32_t fastdiv(uint32_t n, const FastDiv& f) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
+// ---------------------------------------------------------------------------
+// Frustum culling of one warp's box of voxels for one frame, evaluated by the
+// lane whose index is the frame number.  The test is conservative: it only
+// reports "culled" when every voxel of the box is certain to be rejected by
+// the per-voxel test (the projected box lies in the convex hull of its
+// projected corners when no corner is near the camera plane), with a margin
+// of two pixels and 1e-4 in depth that covers rounding.
+template <int MODE>
+__device__ __forceinline__ bool box_culled(const IntegrateArgs& a, const float* fr, int f, int x_lo, int x_hi,
+                                           int y_lo, int y_hi, int z_lo, int z_hi) {
+    const VolDesc& v = a.vol;
+    const FrameDesc& fd = a.frames[f];
+    const float X[2] = {centre(x_lo, v.vs[0], v.off[0]), centre(x_hi, v.vs[0], v.off[0])};
+    const float Y[2] = {centre(y_lo, v.vs[1], v.off[1]), centre(y_hi, v.vs[1], v.off[1])};
+    const float Zw[2] = {centre(z_lo, v.vs[2], v.off[2]), centre(z_hi, v.vs[2], v.off[2])};
+    float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
+    int npos = 0, nneg = 0, nbehind = 0;
+    // depth margin: far above the float rounding of a camera coordinate at this scale
+    const float tmax = (MODE == kCompat) ? fmaxf(fabsf(fr[9]), fmaxf(fabsf(fr[10]), fabsf(fr[11])))
+                                         : fabsf(fr[11]);
+    const float scale = fmaxf(fmaxf(fmaxf(fabsf(X[0]), fabsf(X[1])), fmaxf(fabsf(Y[0]), fabsf(Y[1]))),
+                              fmaxf(fmaxf(fabsf(Zw[0]), fabsf(Zw[1])), tmax));
+    const float eps = 1e-4f + 1e-5f * scale;
+    if (MODE == kCompat) {
+        // world z exactly 0 sends a voxel to pixel (0,0) (camera_util.cu:46): keep such boxes
+        if (!(Zw[0] > 0.f || Zw[1] < 0.f)) return false;
+        if ((Zw[0] > 0.f) != (Zw[1] > 0.f)) return false;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float px = X[k & 1], py = Y[(k >> 1) & 1], pz = Zw[k >> 2];
+        float cx, cy, cz;
+        if (MODE == kCompat) {
+            cx = fr[0] * px + fr[1] * py + fr[2] * pz + fr[9];
+            cy = fr[3] * px + fr[4] * py + fr[5] * pz + fr[10];
+            cz = fr[6] * px + fr[7] * py + fr[8] * pz + fr[11];
+            cx *= v.fx;
+            cy *= v.fy;
+        } else {
+            cx = fr[0] * px + fr[1] * py + fr[2] * pz + fr[3];
+            cy = fr[4] * px + fr[5] * py + fr[6] * pz + fr[7];
+            cz = fr[8] * px + fr[9] * py + fr[10] * pz + fr[11];
+            if (cz <= v.min_z - eps) ++nbehind;
+        }
+        if (cz > eps)
+            ++npos;
+        else if (cz < -eps)
+            ++nneg;
+        const float rz = 1.0f / cz;
+        const float u = cx * rz, w = cy * rz;
+        umin = fminf(umin, u);
+        umax = fmaxf(umax, u);
+        vmin = fminf(vmin, w);
+        vmax = fmaxf(vmax, w);
+    }
+    if (MODE == kFixed) {
+        if (nbehind == 8) return true;
+        // a box reaching behind the camera is only decided by the test above
+        if (npos != 8) return false;
+        // accepted pixels satisfy -0.5 <= u < width - 0.5
+        const float W = (float)fd.width, H = (float)fd.height;
+        return umax < -2.5f || umin > W + 1.5f || vmax < -2.5f || vmin > H + 1.5f;
+    } else {
+        if (npos != 8 && nneg != 8) return false;
+        const float ccx = v.cx, ccy = v.cy;
+        // truncation keeps pixel k for values in (k-1, k+1) around 0 and [k, k+1) elsewhere
+        const float W = (float)fd.width, H = (float)fd.height;
+        return umax + ccx < -3.0f || umin + ccx > W + 2.0f || vmax + ccy < -3.0f || vmin + ccy > H + 2.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Integrate: one CTA of 128 threads per brick of (4*TX) x BY x BZ voxels; a
+// thread owns 4 consecutive voxels along x, moved as one 16-byte load/store
+// of distance and one of weight.  All frames of the pass are applied to the
+// voxels in registers, in frame order, so a voxel sees exactly the sequence
+// of updates the per-frame reference loop would apply.
+template <int MODE, int TX, int BY, int BZ>
+__global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ IntegrateArgs a) {
+    static_assert(TX * BY * BZ == 128, "128 threads per CTA");
+    static_assert(32 % TX == 0, "a warp spans whole x rows");
+    __shared__ float s_pose[GBT_MAX_FRAMES_PER_PASS][12];
+    __shared__ float s_inv[256];
+
+    const VolDesc& v = a.vol;
+    const int tid = threadIdx.x;
+    const int nf = a.nframes;
+    if (tid < nf) {
+        const FrameDesc& fd = a.frames[tid];
+        if (MODE == kCompat) {
+            float R[9];
+            compat_rotation(fd.q, R);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) s_pose[tid][k] = R[k];
+            s_pose[tid][9] = fd.t[0];
+            s_pose[tid][10] = fd.t[1];
+            s_pose[tid][11] = fd.t[2];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 12; ++k) s_pose[tid][k] = fd.P[k];
+        }
+    }
+    if (MODE == kFixed) {
+        for (int k = tid; k < 256; k += 128) s_inv[k] = k ? __frcp_rn((float)k) : 0.f;
+    }
+    __syncthreads();
+
+    const int tx = tid % TX, ty = (tid / TX) % BY, tz = tid / (TX * BY);
+    const int lane = tid & 31;
+    const int wfirst = tid & ~31;
+    // the warp's sub-box inside the brick
+    const int wy_lo = (TX * BY >= 32) ? (wfirst / TX) % BY : 0;
+    const int wy_hi = (TX * BY >= 32) ? wy_lo + 32 / TX - 1 : BY - 1;
+    const int wz_lo = wfirst / (TX * BY);
+    const int wz_hi = (wfirst + 31) / (TX * BY);
+
+    const int nx = v.nx, ny = v.ny, nz = v.nz;
+    const int BXV = 4 * TX;
+    const int nbx = (nx + BXV - 1) / BXV, nby = (ny + BY - 1) / BY, nbz = (nz + BZ - 1) / BZ;
+    const long long nbricks = (long long)nbx * nby * nbz;
+    const bool vec_ok = (nx & 3) == 0;
+    const uint32_t all_frames = nf >= 32 ? 0xffffffffu : ((1u << nf) - 1u);
+
+    for (long long b = blockIdx.x; b < nbricks; b += gridDim.x) {
+        const int bxi = (int)(b % nbx);
+        const long long rest = b / nbx;
+        const int byi = (int)(rest % nby);
+        const int bzi = (int)(rest / nby);
+        const int bx0 = bxi * BXV, by0 = byi * BY, bz0 = bzi * BZ;
+
+        // frames for which this warp's box may contain an updated voxel
+        bool live = false;
+        if (lane < nf) {
+            const int xl = bx0, xh = min(bx0 + BXV, nx) - 1;
+            const int yl = by0 + wy_lo, yh = min(by0 + wy_hi, ny - 1);
+            const int zl = bz0 + wz_lo, zh = min(bz0 + wz_hi, nz - 1);
+            live = (yl <= yh && zl <= zh) && !box_culled<MODE>(a, s_pose[lane], lane, xl, xh, yl, yh, zl, zh);
+        }
+        const uint32_t fmask = __ballot_sync(0xffffffffu, live) & all_frames;
+        if (fmask == 0u) continue;
+
+        const int x0 = bx0 + 4 * tx, y = by0 + ty, z = bz0 + tz;
+        if (y >= ny || z >= nz || x0 >= nx) continue;
+        const size_t base = ((size_t)z * ny + y) * nx + x0;
+        const bool full = vec_ok && (x0 + 3 < nx);
+        float d[4], w[4];
+        if (full) {
+            const float4 d4 = *reinterpret_cast<const float4*>(v.D + base);
+            const float4 w4 = *reinterpret_cast<const float4*>(v.W + base);
+            d[0] = d4.x; d[1] = d4.y; d[2] = d4.z; d[3] = d4.w;
+            w[0] = w4.x; w[1] = w4.y; w[2] = w4.z; w[3] = w4.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                d[i] = (x0 + i < nx) ? v.D[base + i] : 0.f;
+                w[i] = (x0 + i < nx) ? v.W[base + i] : 0.f;
+            }
+        }
+        const float py = centre(y, v.vs[1], v.off[1]);
+        const float pz = centre(z, v.vs[2], v.off[2]);
+        float px[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) px[i] = centre(x0 + i, v.vs[0], v.off[0]);
+        const int nvalid = min(4, nx - x0);
+        bool dirty = false;
+
+        uint32_t m = fmask;
+        while (m) {
+            const int f = __ffs(m) - 1;
+            m &= m - 1;
+            const FrameDesc& fd = a.frames[f];
+            const char* dimg = static_cast<const char*>(fd.depth);
+            const int64_t pitch = fd.pitch;
+            const uint32_t width = (uint32_t)fd.width, height = (uint32_t)fd.height;
+            const float* pr = s_pose[f];
+            if (MODE == kCompat) {
+                const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
+                const float r6 = pr[6], r7 = pr[7], r8 = pr[8], t0 = pr[9], t1 = pr[10], t2 = pr[11];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (i >= nvalid) break;
+                    // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51)
+                    int u = 0, vv = 0;
+                    if (pz != 0.f) {
+                        const float cxv = compat_cam(r0, r1, r2, t0, px[i], py, pz);
+                        const float cyv = compat_cam(r3, r4, r5, t1, px[i], py, pz);
+                        const float czv = compat_cam(r6, r7, r8, t2, px[i], py, pz);
+                        if (czv != 0.f) {
+                            u = (int)compat_q(cxv, v.fx, czv, v.cx);
+                            vv = (int)compat_q(cyv, v.fy, czv, v.cy);
+                        }
+                    }
+                    // tsdf_volume.cu:166-187
+                    if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
+                    const float dv = __ldg(reinterpret_cast<const float*>(dimg + (int64_t)vv * pitch) + u);
+                    if (dv <= 0.0f || dv > 24.0) continue;
+                    const float sdf = dv - pz;
+                    if (sdf >= -v.trunc) {
+                        float tsdf = sdf;
+                        if (sdf > 0) tsdf = fminf(sdf, v.trunc);
+                        const float nw = w[i] + 1.0f;
+                        const float nd = compat_avg(d[i], w[i], tsdf, nw);
+                        w[i] = nw;
+                        d[i] = nd;
+                        dirty = true;
+                    }
+                }
+            } else {
+#if !defined(GBT_REF_ARITH)
+                const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
+                const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
+                const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
+                const int fmt = fd.fmt;
+                const float scale = fd.scale;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (i >= nvalid) break;
+                    const float Z = __fmaf_rn(pr[8], px[i], aZ);
+                    if (!(Z > v.min_z)) continue;
+                    const float U = __fmaf_rn(pr[0], px[i], aU);
+                    const float V = __fmaf_rn(pr[4], px[i], aV);
+                    const float rz = __frcp_rn(Z);
+                    const int u = __float2int_rn(__fmul_rn(U, rz));
+                    const int vv = __float2int_rn(__fmul_rn(V, rz));
+                    if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
+                    const char* row = dimg + (int64_t)vv * pitch;
+                    float dv;
+                    if (fmt == GBT_DEPTH_U16)
+                        dv = __fmul_rn((float)__ldg(reinterpret_cast<const unsigned short*>(row) + u), scale);
+                    else
+                        dv = __ldg(reinterpret_cast<const float*>(row) + u);
+                    if (!(dv > 0.f && dv <= v.max_depth)) continue;
+                    const float sdf = __fsub_rn(dv, Z);
+                    if (!(sdf >= -v.trunc)) continue;
+                    const float tsdf = fminf(sdf, v.trunc);
+                    const int n = max(__float2int_rz(w[i]), 0) + 1;
+                    const float inv = n < 256 ? s_inv[n] : __frcp_rn((float)n);
+                    d[i] = __fmaf_rn(__fsub_rn(tsdf, d[i]), inv, d[i]);
+                    w[i] = fminf(__fadd_rn(w[i], 1.0f), v.max_weight);
+                    dirty = true;
+                }
+#endif
+            }
+        }
+        if (!dirty) continue;
+        if (full) {
+            *reinterpret_cast<float4*>(v.D + base) = make_float4(d[0], d[1], d[2], d[3]);
+            *reinterpret_cast<float4*>(v.W + base) = make_float4(w[0], w[1], w[2], w[3]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (x0 + i < nx) {
+                    v.D[base + i] = d[i];
+                    v.W[base + i] = w[i];
+                }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Marching cubes.  Corner k of a cube at (x, y, z) is (x + kDx[k], y + kDy[k],
+// layer z + kDz[k]) in the reference's numbering (marching_cubes.cu:118-127).
+__device__ __forceinline__ int corner_dx(int k) { return (0x66 >> k) & 1; }
+__device__ __forceinline__ int corner_dy(int k) { return (0xF0 >> k) & 1; }
+__device__ __forceinline__ int corner_dz(int k) { return (0xCC >> k) & 1; }
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+constexpr unsigned long long kFlagAgg = 1ull << 62;
+constexpr unsigned long long kFlagIncl = 2ull << 62;
+constexpr unsigned long long kValueMask = (1ull << 62) - 1;
+constexpr int kLookbackSpinLimit = 1 << 22;
+
+// Linear index of corner 0 of cube (cx, cy, cz) and of the next layer.
+template <int MODE>
+__device__ __forceinline__ void cube_base(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int64_t* b0,
+                                          int64_t* b1) {
+    const int64_t gx = a.gx;
+    const int64_t layer = (MODE == kCompat) ? (gx + a.gy) : gx * a.gy;   // marching_cubes.cu:211
+    *b0 = (int64_t)cz * layer + (int64_t)cy * gx + cx;
+    *b1 = *b0 + layer;
+}
+
+template <int MODE>
+__device__ __forceinline__ int64_t corner_index(const McArgs& a, int64_t b0, int64_t b1, int k) {
+    return (corner_dz(k) ? b1 : b0) + corner_dx(k) + (corner_dy(k) ? a.gx : 0);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McArgs a) {
+    __shared__ unsigned char s_count[256];
+    __shared__ unsigned long long s_tri[256];
+    __shared__ unsigned char s_ends[12];
+    __shared__ int s_wsum[kMcCubesPerThread * (kMcThreads / 32)];
+    __shared__ unsigned int s_tile;
+    __shared__ long long s_prefix;
+
+    const int tid = threadIdx.x;
+    for (int k = tid; k < 256; k += kMcThreads) {
+        s_count[k] = GBT_MC_TRI_COUNT[k];
+        s_tri[k] = GBT_MC_TRI_PACKED[k];
+    }
+    if (tid < 12) s_ends[tid] = GBT_MC_EDGE_ENDS[tid];
+    const int lane = tid & 31, warp = tid >> 5;
+    constexpr int kWarps = kMcThreads / 32;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= a.ntiles) return;
+        const uint32_t c0 = tile * (uint32_t)kMcTile;
+
+        int type[kMcCubesPerThread];
+        int incl[kMcCubesPerThread];
+#pragma unroll
+        for (int i = 0; i < kMcCubesPerThread; ++i) {
+            const uint32_t c = c0 + i * kMcThreads + tid;
+            int t = 0;
+            if (c < a.ncubes) {
+                const uint32_t row = fastdiv(c, a.div_cx);
+                const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
+                const uint32_t cz = fastdiv(row, a.div_cy);
+                const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+                int64_t b0, b1;
+                cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+                bool ok = true;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int64_t idx = corner_index<MODE>(a, b0, b1, k);
+                    if (MODE == kFixed) ok = ok && (__ldg(a.W + idx) > 0.f);
+                    if (__ldg(a.D + idx) < 0.f) t |= 1 << k;
+                }
+                if (!ok) t = 0;
+            }
+            type[i] = t;
+            int n = s_count[t];
+            // inclusive warp scan
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, n, o);
+                if (lane >= o) n += y;
+            }
+            incl[i] = n;
+            if (lane == 31) s_wsum[i * kWarps + warp] = n;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // exclusive scan of the (i, warp) partial sums, in linear cube order
+            constexpr int kParts = kMcCubesPerThread * kWarps;
+            static_assert(kParts <= 32, "one warp scans the partial sums");
+            int s = lane < kParts ? s_wsum[lane] : 0;
+            int x = s;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, x, 31);
+            if (lane < kParts) s_wsum[lane] = x - s;
+            if (lane == 0) {
+                // decoupled look-back over the preceding tiles
+                long long prefix = 0;
+                if (tile == 0) {
+                    st_release(a.status + tile, kFlagIncl | (unsigned long long)total);
+                } else {
+                    st_release(a.status + tile, kFlagAgg | (unsigned long long)total);
+                    int64_t j = (int64_t)tile - 1;
+                    int spins = 0;
+                    while (j >= 0) {
+                        const unsigned long long w = ld_acquire(a.status + j);
+                        const unsigned long long flag = w & ~kValueMask;
+                        if (flag == 0ull) {
+                            if (++spins > kLookbackSpinLimit) {
+                                atomicExch(a.error, 1);
+                                break;
+                            }
+                            __nanosleep(64);
+                            continue;
+                        }
+                        prefix += (long long)(w & kValueMask);
+                        if (flag == kFlagIncl) break;
+                        --j;
+                    }
+                    st_release(a.status + tile, kFlagIncl | (unsigned long long)(prefix + total));
+                }
+                s_prefix = prefix;
+                if (tile == a.ntiles - 1) *a.total = prefix + total;
+            }
+        }
+        __syncthreads();
+        if (a.cap <= 0) continue;
+        const long long tile_prefix = s_prefix;
+
+#pragma unroll
+        for (int i = 0; i < kMcCubesPerThread; ++i) {
+            const int t = type[i];
+            const int n = s_count[t];
+            if (!n) continue;
+            long long out = tile_prefix + s_wsum[i * kWarps + warp] + incl[i] - n;
+            if (out >= a.cap) continue;
+            const uint32_t c = c0 + i * kMcThreads + tid;
+            const uint32_t row = fastdiv(c, a.div_cx);
+            const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
+            const uint32_t cz = fastdiv(row, a.div_cy);
+            const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+            int64_t b0, b1;
+            cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+            float val[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) val[k] = __ldg(a.D + corner_index<MODE>(a, b0, b1, k));
+            const unsigned long long edges = s_tri[t];
+            for (int tr = 0; tr < n; ++tr, ++out) {
+                if (out >= a.cap) break;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const int e = (int)((edges >> (4 * (3 * tr + j))) & 15ull);
+                    int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
+                    float pa[3], pb[3];
+                    float sa = val[ca], sb = val[cb];
+                    if (MODE == kCompat) {
+                        if (sa > 0 && sb < 0) {  // marching_cubes.cu:34-41
+                            const int tc = ca; ca = cb; cb = tc;
+                            const float ts = sa; sa = sb; sb = ts;
+                        }
+                        // corner positions come from the voxel at the same linear index
+                        const int64_t ia = corner_index<MODE>(a, b0, b1, ca);
+                        const int64_t ib = corner_index<MODE>(a, b0, b1, cb);
+                        const uint32_t ra = fastdiv((uint32_t)ia, a.div_gx), rb = fastdiv((uint32_t)ib, a.div_gx);
+                        const uint32_t za = fastdiv(ra, a.div_gy), zb = fastdiv(rb, a.div_gy);
+                        pa[0] = centre((int)((uint32_t)ia - ra * (uint32_t)a.gx), a.vs[0], a.off[0]);
+                        pa[1] = centre((int)(ra - za * (uint32_t)a.gy), a.vs[1], a.off[1]);
+                        pa[2] = centre((int)za, a.vs[2], a.off[2]);
+                        pb[0] = centre((int)((uint32_t)ib - rb * (uint32_t)a.gx), a.vs[0], a.off[0]);
+                        pb[1] = centre((int)(rb - zb * (uint32_t)a.gy), a.vs[1], a.off[1]);
+                        pb[2] = centre((int)zb, a.vs[2], a.off[2]);
+                        const float r = mc_ratio(sa, sb);
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) a.verts[9 * out + 3 * j + q] = mc_lerp(pa[q], pb[q], r);
+                    } else {
+#if !defined(GBT_REF_ARITH)
+                        // lower endpoint first, so the cubes sharing the edge agree
+                        if (corner_dx(ca) + corner_dy(ca) + corner_dz(ca) > corner_dx(cb) + corner_dy(cb) + corner_dz(cb)) {
+                            const int tc = ca; ca = cb; cb = tc;
+                            const float ts = sa; sa = sb; sb = ts;
+                        }
+                        pa[0] = centre((int)cx + corner_dx(ca), a.vs[0], a.off[0]);
+                        pa[1] = centre((int)cy + corner_dy(ca), a.vs[1], a.off[1]);
+                        pa[2] = centre((int)cz + corner_dz(ca), a.vs[2], a.off[2]);
+                        pb[0] = centre((int)cx + corner_dx(cb), a.vs[0], a.off[0]);
+                        pb[1] = centre((int)cy + corner_dy(cb), a.vs[1], a.off[1]);
+                        pb[2] = centre((int)cz + corner_dz(cb), a.vs[2], a.off[2]);
+                        const float r = __fdiv_rn(sa, __fsub_rn(sa, sb));
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) a.verts[9 * out + 3 * j + q] = __fmaf_rn(r, __fsub_rn(pb[q], pa[q]), pa[q]);
+#endif
+                    }
+                    a.tris[3 * out + j] = (int32_t)(a.index_base + 3 * out + j);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int MODE, int TX, int BY, int BZ>
+cudaError_t launch_integrate_shape(const IntegrateArgs& a, int grid, cudaStream_t s) {
+    integrate_kernel<MODE, TX, BY, BZ><<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_integrate_mode(const IntegrateArgs& a, int brick, int grid, cudaStream_t s) {
+    switch (brick) {
+        case 1: return launch_integrate_shape<MODE, 4, 8, 4>(a, grid, s);
+        case 2: return launch_integrate_shape<MODE, 8, 2, 8>(a, grid, s);
+        case 3: return launch_integrate_shape<MODE, 16, 2, 4>(a, grid, s);
+        default: return launch_integrate_shape<MODE, 8, 4, 4>(a, grid, s);
+    }
+}
+
+template <int MODE>
+cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
+    static int sms = 0, per_sm = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<MODE>, kMcThreads, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
+    long long grid = (long long)sms * per_sm;
+    if (grid > (long long)a.ntiles) grid = a.ntiles;
+    if (grid < 1) grid = 1;
+    mc_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace gbt

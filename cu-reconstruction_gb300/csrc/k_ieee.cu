@@ -1,0 +1,20 @@
+// Compat mode in IEEE arithmetic (the CPU oracle's operations) and the fixed
+// mode.  Compiled without fast math; every floating-point operation on the
+// data path is an explicit round-to-nearest intrinsic.
+#include "gbt_kernels.cuh"
+
+namespace gbt {
+
+cudaError_t launch_integrate_compat_ieee(const IntegrateArgs& a, int brick, int grid, cudaStream_t s) {
+    return launch_integrate_mode<kCompat>(a, brick, grid, s);
+}
+
+cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, cudaStream_t s) {
+    return launch_integrate_mode<kFixed>(a, brick, grid, s);
+}
+
+cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kCompat>(a, s); }
+
+cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kFixed>(a, s); }
+
+}  // namespace gbt

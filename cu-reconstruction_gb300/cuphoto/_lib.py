@@ -1,0 +1,123 @@
+"""ctypes view of the engine's C ABI (include/gbt_tsdf.h).
+
+The shared library is built in-tree by ``cu-reconstruction_gb300/build.py``
+(``__graft_entry__.build()`` runs it).  There is no fallback: if the library
+is missing, :func:`lib` raises.
+"""
+import ctypes as C
+import os
+import threading
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libgbt_tsdf.so")
+
+GBT_OK = 0
+GBT_ERR_INVALID_ARG = 1
+GBT_ERR_CUDA = 2
+GBT_ERR_ALLOC = 3
+GBT_ERR_CAPACITY = 4
+GBT_ERR_TIMEOUT = 5
+
+MODE_COMPAT = 0
+MODE_FIXED = 1
+ARITH_REFERENCE = 0
+ARITH_IEEE = 1
+DEPTH_F32_M = 0
+DEPTH_U16 = 1
+MEMORY_DEVICE = 0
+MEMORY_MANAGED = 1
+MAX_FRAMES_PER_PASS = 32
+
+
+class VolumeCfg(C.Structure):
+    _fields_ = [
+        ("voxel_grid_size", C.c_uint32 * 3),
+        ("physical_size", C.c_float * 3),
+        ("global_offset", C.c_float * 3),
+        ("max_weight", C.c_float),
+        ("focal_x", C.c_float), ("focal_y", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+        ("camera_width", C.c_uint32), ("camera_height", C.c_uint32),
+        ("max_cell_size", C.c_float),
+        ("mode", C.c_int32),
+        ("arith", C.c_int32),
+        ("truncation", C.c_float),
+        ("max_depth", C.c_float),
+        ("min_z", C.c_float),
+        ("memory", C.c_int32),
+    ]
+
+
+class VolumeInfo(C.Structure):
+    _fields_ = [
+        ("voxel_grid_size", C.c_uint32 * 3),
+        ("voxel_size", C.c_float * 3),
+        ("truncation", C.c_float),
+        ("global_offset", C.c_float * 3),
+        ("physical_size", C.c_float * 3),
+        ("num_voxels", C.c_int64),
+        ("tsdf", C.c_void_p),
+        ("weights", C.c_void_p),
+        ("mode", C.c_int32),
+        ("arith", C.c_int32),
+    ]
+
+
+class Frame(C.Structure):
+    _fields_ = [
+        ("depth", C.c_void_p),
+        ("pitch_bytes", C.c_size_t),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("format", C.c_int32),
+        ("depth_scale", C.c_float),
+        ("pose", C.c_double * 7),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point, in header order.
+SIGNATURES = [
+    ("gbt_volume_create", C.c_int, [C.POINTER(VolumeCfg), C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("gbt_volume_destroy", C.c_int, [C.c_void_p]),
+    ("gbt_volume_reset", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("gbt_volume_get_info", C.c_int, [C.c_void_p, C.POINTER(VolumeInfo)]),
+    ("gbt_volume_transformation_voxels", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("gbt_integrate", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_void_p]),
+    ("gbt_integrate_tuned", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    ("gbt_extract_mesh", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                   C.POINTER(C.c_int64), C.c_void_p]),
+    ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                         C.c_void_p, C.c_void_p]),
+    ("gbt_last_error", C.c_char_p, []),
+    ("gbt_version", C.c_char_p, []),
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GbtError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("gbt status %d: %s" % (status, message))
+        self.status = status
+
+
+def lib():
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError("engine library %s is missing; run cu-reconstruction_gb300/build.py "
+                                   "(or __graft_entry__.build()) first" % LIB_PATH)
+            handle = C.CDLL(LIB_PATH)
+            for name, res, args in SIGNATURES:
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+        return _lib
+
+
+def check(status):
+    if status != GBT_OK:
+        raise GbtError(status, lib().gbt_last_error().decode())
+    return status

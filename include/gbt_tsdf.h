@@ -1,0 +1,177 @@
+/*
+ * gbt_tsdf.h -- C ABI of the GB300 TSDF surface-fusion engine.
+ *
+ * This is the drop-in boundary for the TSDF path of cu-Reconstruction
+ * (namespace cuphoto).  The reference has no C ABI: its entry points are the
+ * C++ members of cuphoto::TSDFVolume and the free function
+ * cuphoto::generate_triangular_surface.  Each entry point below names the
+ * reference interface it replaces; the C++ shim in
+ * cu-reconstruction_gb300/cpp/ rebuilds those C++ signatures on top of it.
+ *
+ * Conventions
+ *   - Every function returns a gbt_status; on failure gbt_last_error() gives a
+ *     message for the calling thread.
+ *   - Depth images, mesh buffers and streams are borrowed: device pointers
+ *     that must stay valid until the work queued on `stream` has finished.
+ *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy default
+ *     stream.  Calls are asynchronous unless documented otherwise.
+ *   - A volume must not be used from two host threads at once.
+ */
+#ifndef GBT_TSDF_H
+#define GBT_TSDF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBT_OK = 0,
+    GBT_ERR_INVALID_ARG = 1,   /* bad pointer, size or configuration */
+    GBT_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    GBT_ERR_ALLOC = 3,         /* device allocation failed */
+    GBT_ERR_CAPACITY = 4,      /* output buffer too small: counts are valid, output truncated */
+    GBT_ERR_TIMEOUT = 5        /* a bounded device-side wait gave up; results are invalid */
+} gbt_status;
+
+typedef enum {
+    /* Reproduces the reference's arithmetic and quirks: SDF against world z,
+     * truncating pixel cast, no weight clamp, mesh layer stride gx+gy,
+     * three vertices per triangle (tsdf_volume.cu:144-190, marching_cubes.cu:191-237). */
+    GBT_MODE_COMPAT = 0,
+    /* Geometrically corrected: camera-space SDF, nearest pixel, cameras
+     * looking away rejected, weight clamped at max_weight, true layer stride,
+     * cubes touching unobserved voxels skipped. */
+    GBT_MODE_FIXED = 1
+} gbt_mode;
+
+typedef enum {
+    /* Divisions compiled as the reference compiles them (-use_fast_math):
+     * bit-exact with the reference's own GPU build. */
+    GBT_ARITH_REFERENCE = 0,
+    /* Correctly rounded IEEE divisions, no flush-to-zero: bit-exact with the
+     * CPU oracle. */
+    GBT_ARITH_IEEE = 1
+} gbt_arith;
+
+typedef enum {
+    GBT_DEPTH_F32_M = 0,   /* float metres (the reference's CV_32F depth) */
+    GBT_DEPTH_U16 = 1      /* uint16 raw units, metres = raw * depth_scale; 0 = no depth */
+} gbt_depth_format;
+
+typedef enum {
+    GBT_MEMORY_DEVICE = 0,   /* cudaMalloc */
+    GBT_MEMORY_MANAGED = 1   /* cudaMallocManaged, host-readable as in the reference */
+} gbt_memory;
+
+/* Mirrors cuphoto::TSDFVolumeConfig (tsdf_volume.cuh:17-29) plus the engine's
+ * own options after max_cell_size.  Zero-initialise, then set fields. */
+typedef struct {
+    uint32_t voxel_grid_size[3];
+    float physical_size[3];
+    float global_offset[3];
+    float max_weight;          /* fixed mode: weight clamp; compat: unused (as in the reference) */
+    float focal_x, focal_y, cx, cy;
+    uint32_t camera_width, camera_height;   /* informational, as in the reference */
+    float max_cell_size;                   /* unused, as in the reference */
+    /* engine options */
+    int32_t mode;              /* gbt_mode */
+    int32_t arith;             /* gbt_arith, compat mode only */
+    float truncation;          /* <= 0: 1.1 * |voxel size| (tsdf_volume.cu:199) */
+    float max_depth;           /* <= 0: 24 m (tsdf_volume.cu:169) */
+    float min_z;               /* fixed mode: nearest accepted camera depth; 0 means z > 0 */
+    int32_t memory;            /* gbt_memory */
+} gbt_volume_cfg;
+
+/* Derived values a caller may need (voxel size and truncation as computed by
+ * the reference's constructor, tsdf_volume.cu:197-199). */
+typedef struct {
+    uint32_t voxel_grid_size[3];
+    float voxel_size[3];
+    float truncation;
+    float global_offset[3];
+    float physical_size[3];
+    int64_t num_voxels;
+    float* tsdf;               /* device (or managed) pointer, x fastest */
+    float* weights;
+    int32_t mode;
+    int32_t arith;
+} gbt_volume_info;
+
+/* One depth frame.  pose = {qw, qx, qy, qz, tx, ty, tz}, the world-to-camera
+ * transform, in the order of TSDFVolume::integrate (tsdf_volume.cu:257-272). */
+typedef struct {
+    const void* depth;         /* device pointer */
+    size_t pitch_bytes;        /* row stride in bytes */
+    int32_t width, height;
+    int32_t format;            /* gbt_depth_format */
+    float depth_scale;         /* GBT_DEPTH_U16 only */
+    double pose[7];
+} gbt_frame;
+
+typedef struct gbt_volume gbt_volume;
+
+/* Replaces TSDFVolume::TSDFVolume + setup_data (tsdf_volume.cu:194-212,227-254):
+ * allocates the distance and weight grids and initialises them (distance =
+ * truncation, weight = 0).  Synchronises `stream` before returning. */
+gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume** out);
+
+/* Replaces TSDFVolume::~TSDFVolume (tsdf_volume.cu:214-224). */
+gbt_status gbt_volume_destroy(gbt_volume* vol);
+
+/* Re-runs setup_data (tsdf_volume.cu:227-254) on `stream`. */
+gbt_status gbt_volume_reset(gbt_volume* vol, void* stream);
+
+/* Replaces the accessors voxel_distances_data, voxel_weights_data,
+ * voxel_grid_size, global_offset, scale_voxel_size, voxel_phys_size
+ * (tsdf_volume.cuh:57-83). */
+gbt_status gbt_volume_get_info(const gbt_volume* vol, gbt_volume_info* info);
+
+/* Replaces transformation_voxels_data (tsdf_volume.cuh:86-92).  The engine
+ * never stores the per-voxel {float3 centre, float4 quaternion} records; the
+ * first call materialises them (28 bytes per voxel, packed as in
+ * tsdf_volume.cuh:33-38) and later calls return the same buffer. */
+gbt_status gbt_volume_transformation_voxels(gbt_volume* vol, void* stream, void** out);
+
+/* Replaces TSDFVolume::integrate(color, depth, pose) (tsdf_volume.cu:257-290)
+ * for `nframes` frames at once: the frames are applied in order, in one
+ * pass over the volume (distance and weight read and written once).
+ * nframes may be 1..GBT_MAX_FRAMES_PER_PASS.  Asynchronous. */
+#define GBT_MAX_FRAMES_PER_PASS 32
+gbt_status gbt_integrate(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, void* stream);
+
+/* Same as gbt_integrate with an explicit tile shape and grid size, for the
+ * autotuner.  brick: 0 = 32x4x4 voxels, 1 = 16x8x4, 2 = 32x2x8, 3 = 64x2x4.
+ * ctas_per_sm: 0 = default. */
+gbt_status gbt_integrate_tuned(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, int32_t brick,
+                               int32_t ctas_per_sm, void* stream);
+
+/* Replaces generate_triangular_surface (marching_cubes.cu:191-237).
+ * Writes up to cap_tris triangles: verts gets 9 floats per triangle (three
+ * vertices, no sharing, as the reference emits them) and tris gets 3 ints per
+ * triangle, (index_base + 3t, +1, +2).  *n_tris receives the full count.
+ * Triangles come out in the reference's order: cube z, y, x, then table order.
+ * Synchronises `stream`.  Returns GBT_ERR_CAPACITY if the count exceeds cap_tris
+ * (the first cap_tris triangles are still written).  verts/tris may be NULL
+ * when cap_tris is 0 (count only). */
+gbt_status gbt_extract_mesh(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
+                            int64_t* n_tris, void* stream);
+
+/* Asynchronous form of gbt_extract_mesh: the count is written to the device
+ * word *d_n_tris and nothing is synchronised; usable inside stream capture. */
+gbt_status gbt_extract_mesh_async(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
+                                  int64_t index_base, int64_t* d_n_tris, void* stream);
+
+/* Message for the last failure on the calling thread ("" if none). */
+const char* gbt_last_error(void);
+
+/* Engine version string. */
+const char* gbt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBT_TSDF_H */

@@ -1,0 +1,233 @@
+"""Python access to the CPU oracle and to the reference's own kernels.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker.  The engine never imports it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+HARNESS_SO = os.path.join(HERE, "_build", "libref_harness.so")
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_tsdf.cubin")
+REF_NAMES = os.path.join(HERE, "_ref", "ref_kernels.txt")
+
+
+class OracleCfg(C.Structure):
+    _fields_ = [
+        ("grid", C.c_int32 * 3),
+        ("phys", C.c_float * 3),
+        ("offset", C.c_float * 3),
+        ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+        ("max_weight", C.c_float),
+        ("truncation", C.c_float),
+        ("max_depth", C.c_float),
+        ("min_z", C.c_float),
+    ]
+
+
+_so = None
+
+
+def ensure_built():
+    """Builds the oracle (and the reference kernels where possible) if stale."""
+    import importlib
+    return importlib.import_module(__name__ + ".build").build_all()
+
+
+def lib():
+    global _so
+    if _so is None:
+        if not os.path.exists(ORACLE_SO):
+            ensure_built()
+        so = C.CDLL(ORACLE_SO)
+        f, d, i32, i64, vp = C.c_float, C.c_double, C.c_int32, C.c_int64, C.c_void_p
+        P = C.POINTER
+        so.oracle_derive.argtypes = [P(OracleCfg), vp, vp]
+        so.oracle_volume_init.argtypes = [P(OracleCfg), vp, vp]
+        so.oracle_integrate_compat.argtypes = [P(OracleCfg), vp, vp, vp, i64, i32, i32, vp, i32]
+        so.oracle_compat_ambiguous.argtypes = [P(OracleCfg), vp, i32, i32, f, vp, i32]
+        so.oracle_integrate_fixed.argtypes = [P(OracleCfg), vp, vp, vp, i64, i32, i32, i32, f, vp, i32]
+        so.oracle_mc_compat.argtypes = [P(OracleCfg), vp, vp, vp, i64, i64, i32]
+        so.oracle_mc_compat.restype = i64
+        so.oracle_mc_fixed.argtypes = [P(OracleCfg), vp, vp, vp, vp, i64, i64, i32]
+        so.oracle_mc_fixed.restype = i64
+        _so = so
+    return _so
+
+
+def cfg_from(tc):
+    """OracleCfg from a cuphoto.TSDFVolumeConfig (or any object with its fields)."""
+    c = OracleCfg()
+    for i in range(3):
+        c.grid[i] = int(tc.voxel_grid_size[i])
+        c.phys[i] = float(tc.physical_size[i])
+        c.offset[i] = float(tc.global_offset[i])
+    c.fx, c.fy, c.cx, c.cy = float(tc.focal_x), float(tc.focal_y), float(tc.cx), float(tc.cy)
+    c.max_weight = float(tc.max_weight)
+    c.truncation = float(getattr(tc, "truncation", 0.0))
+    c.max_depth = float(getattr(tc, "max_depth", 0.0))
+    c.min_z = float(getattr(tc, "min_z", 0.0))
+    return c
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def derive(cfg):
+    vs = np.zeros(3, np.float32)
+    tr = np.zeros(1, np.float32)
+    lib().oracle_derive(C.byref(cfg), _p(vs), _p(tr))
+    return vs, float(tr[0])
+
+
+def init_volume(cfg):
+    n = cfg.grid[0] * cfg.grid[1] * cfg.grid[2]
+    D = np.empty(n, np.float32)
+    W = np.empty(n, np.float32)
+    lib().oracle_volume_init(C.byref(cfg), _p(D), _p(W))
+    shape = (cfg.grid[2], cfg.grid[1], cfg.grid[0])
+    return D.reshape(shape), W.reshape(shape)
+
+
+def _pose(pose):
+    return np.ascontiguousarray(pose, np.float64)
+
+
+def integrate_compat(cfg, D, W, depth_m, pose, threads=0):
+    depth_m = np.ascontiguousarray(depth_m, np.float32)
+    p = _pose(pose)
+    lib().oracle_integrate_compat(C.byref(cfg), _p(D), _p(W), _p(depth_m), depth_m.strides[0],
+                                  depth_m.shape[1], depth_m.shape[0], _p(p), threads)
+
+
+def compat_ambiguous(cfg, pose, width, height, ulps=8.0, flags=None, threads=0):
+    n = cfg.grid[0] * cfg.grid[1] * cfg.grid[2]
+    if flags is None:
+        flags = np.zeros((cfg.grid[2], cfg.grid[1], cfg.grid[0]), np.uint8)
+    p = _pose(pose)
+    lib().oracle_compat_ambiguous(C.byref(cfg), _p(p), width, height, float(ulps), _p(flags), threads)
+    return flags
+
+
+def integrate_fixed(cfg, D, W, depth, pose, depth_scale=0.001, threads=0):
+    depth = np.ascontiguousarray(depth)
+    fmt = 1 if depth.dtype in (np.uint16, np.int16) else 0
+    if fmt == 0:
+        depth = depth.astype(np.float32, copy=False)
+    p = _pose(pose)
+    lib().oracle_integrate_fixed(C.byref(cfg), _p(D), _p(W), _p(depth), depth.strides[0], depth.shape[1],
+                                 depth.shape[0], fmt, float(depth_scale), _p(p), threads)
+
+
+def mc_compat(cfg, D, index_base=0, threads=0):
+    n = lib().oracle_mc_compat(C.byref(cfg), _p(D), None, None, 0, index_base, threads)
+    V = np.empty((max(n, 1), 3, 3), np.float32)
+    T = np.empty((max(n, 1), 3), np.int32)
+    lib().oracle_mc_compat(C.byref(cfg), _p(D), _p(V), _p(T), n, index_base, threads)
+    return V[:n], T[:n]
+
+
+def mc_fixed(cfg, D, W, index_base=0, threads=0):
+    n = lib().oracle_mc_fixed(C.byref(cfg), _p(D), _p(W), None, None, 0, index_base, threads)
+    V = np.empty((max(n, 1), 3, 3), np.float32)
+    T = np.empty((max(n, 1), 3), np.int32)
+    lib().oracle_mc_fixed(C.byref(cfg), _p(D), _p(W), _p(V), _p(T), n, index_base, threads)
+    return V[:n], T[:n]
+
+
+# ---------------------------------------------------------------------------
+class RefHarness:
+    """The reference's own kernels (compiled from its sources) driven with its
+    host-side logic.  Needs a GPU and oracle/_ref/ref_tsdf.cubin."""
+
+    _so = None
+
+    @classmethod
+    def available(cls):
+        return os.path.exists(REF_CUBIN) and os.path.exists(REF_NAMES) and os.path.exists(HARNESS_SO)
+
+    @classmethod
+    def lib(cls):
+        if cls._so is None:
+            so = C.CDLL(HARNESS_SO)
+            vp, i32, i64, f = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+            so.ref_last_error.restype = C.c_char_p
+            so.ref_load.argtypes = [C.c_char_p, C.c_char_p]
+            so.ref_volume_create.argtypes = [vp, vp, vp, f, f, f, f, f, C.POINTER(vp)]
+            so.ref_volume_destroy.argtypes = [vp]
+            so.ref_truncation.argtypes = [vp]
+            so.ref_truncation.restype = f
+            so.ref_integrate.argtypes = [vp, vp, C.c_size_t, i32, i32, vp, C.POINTER(f)]
+            so.ref_read_volume.argtypes = [vp, vp, vp]
+            so.ref_write_distances.argtypes = [vp, vp]
+            so.ref_extract.argtypes = [vp, vp, vp, i64, C.POINTER(f)]
+            so.ref_extract.restype = i64
+            if so.ref_load(REF_CUBIN.encode(), REF_NAMES.encode()) != 0:
+                raise RuntimeError("reference kernels: " + so.ref_last_error().decode())
+            cls._so = so
+        return cls._so
+
+    def __init__(self, tc):
+        so = self.lib()
+        self.grid = np.array(tc.voxel_grid_size, np.uint32)
+        phys = np.array(tc.physical_size, np.float32)
+        off = np.array(tc.global_offset, np.float32)
+        self.h = C.c_void_p()
+        if so.ref_volume_create(_p(self.grid), _p(phys), _p(off), float(tc.max_weight), float(tc.focal_x),
+                                float(tc.focal_y), float(tc.cx), float(tc.cy), C.byref(self.h)) != 0:
+            raise RuntimeError("reference volume: " + so.ref_last_error().decode())
+
+    def close(self):
+        if self.h and self.h.value:
+            self.lib().ref_volume_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def truncation(self):
+        return self.lib().ref_truncation(self.h)
+
+    def integrate(self, depth_ptr, pitch, width, height, pose):
+        """depth_ptr: device float32 metres.  Returns the kernel time in ms."""
+        p = _pose(pose)
+        ms = C.c_float()
+        if self.lib().ref_integrate(self.h, C.c_void_p(depth_ptr), pitch, width, height, _p(p), C.byref(ms)) != 0:
+            raise RuntimeError(self.lib().ref_last_error().decode())
+        return ms.value
+
+    def read(self):
+        n = int(np.prod(self.grid.astype(np.int64)))
+        D = np.empty(n, np.float32)
+        W = np.empty(n, np.float32)
+        if self.lib().ref_read_volume(self.h, _p(D), _p(W)) != 0:
+            raise RuntimeError(self.lib().ref_last_error().decode())
+        shape = (int(self.grid[2]), int(self.grid[1]), int(self.grid[0]))
+        return D.reshape(shape), W.reshape(shape)
+
+    def write_distances(self, D):
+        D = np.ascontiguousarray(D, np.float32)
+        if self.lib().ref_write_distances(self.h, _p(D)) != 0:
+            raise RuntimeError(self.lib().ref_last_error().decode())
+
+    def extract(self, cap=None):
+        so = self.lib()
+        ms = C.c_float()
+        if cap is None:
+            cap = 0
+        V = np.empty((max(cap, 1), 3, 3), np.float32)
+        T = np.empty((max(cap, 1), 3), np.int32)
+        n = so.ref_extract(self.h, _p(V), _p(T), cap, C.byref(ms))
+        if n < 0:
+            raise RuntimeError(so.ref_last_error().decode())
+        if n > cap:
+            return self.extract(int(n))
+        return V[:n], T[:n], ms.value

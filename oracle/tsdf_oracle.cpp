@@ -1,0 +1,517 @@
+// CPU oracle for the TSDF integrate + marching-cubes path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA engine is
+// compared against; the engine never links, loads or calls it.  Only the test
+// suite, the smoke check and the CPU-baseline leg of the benchmark use it.
+//
+// It restates, in plain C++ on the host, the arithmetic of the reference
+// (SokratG/cu-Reconstruction):
+//
+//   compat integrate   modules/src/cuda/tsdf_volume.cu:144-190 (cu_tsdf_integrate)
+//                      + camera_util.cu:7-19,44-51 (camera_to_pixel, world_to_pixel)
+//                      + se3.cuh:125-140,165-183,207-223 (SE3 from quaternion, R*p+t)
+//   volume set-up      tsdf_volume.cu:194-212,227-254 (voxel size, truncation, init)
+//   compat mesh        marching_cubes.cu:23-157 (per-cube classification and
+//                      edge interpolation) + :159-237 (layer loop, host assembly)
+//
+// The reference is compiled with -use_fast_math, so its divisions are the
+// GPU's approximate divide.  The oracle does NOT imitate that: every division
+// here is an IEEE division, and every multiply-add that nvcc contracts in the
+// reference is written as an explicit fmaf.  The engine's "IEEE" compat
+// variant follows exactly these operations and must match this file bit for
+// bit; the engine's reference-arithmetic variant is checked against the
+// reference's own GPU build instead, and against this file up to the pixel
+// indices flagged by oracle_compat_ambiguous().
+//
+// The "fixed" mode is the engine's geometrically corrected variant (camera
+// space SDF, nearest-pixel rounding, weight clamp, true z-layer stride); it is
+// restated here operation for operation as the engine defines it.
+//
+// Build with -ffp-contract=off so the compiler adds no contraction of its own.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define GBT_MC_CONST static const
+#include "../cu-reconstruction_gb300/csrc/mc_tables.inc"
+GBT_MC_TABLE_DATA
+
+extern "C" {
+
+typedef struct {
+    int32_t grid[3];
+    float phys[3];
+    float offset[3];
+    float fx, fy, cx, cy;
+    float max_weight;
+    float truncation;  // <= 0: the reference's 1.1 * |voxel size|
+    float max_depth;   // <= 0: the reference's 24 m
+    float min_z;       // fixed mode: nearest accepted camera depth (> 0 strict when 0)
+} oracle_cfg;
+
+}  // extern "C"
+
+namespace {
+
+struct Derived {
+    float vs[3];
+    float trunc;
+    float max_depth;
+    int64_t nx, ny, nz;
+};
+
+// tsdf_volume.cu:197 (voxel_size = physical_size / grid, cudaMath.cuh:1225)
+// and :199 (1.1f * length(voxel_size), cudaMath.cuh:1487,1530).
+Derived derive(const oracle_cfg* c) {
+    Derived d;
+    for (int i = 0; i < 3; ++i) d.vs[i] = c->phys[i] / (float)(uint32_t)c->grid[i];
+    float dot = d.vs[0] * d.vs[0] + d.vs[1] * d.vs[1];
+    dot = dot + d.vs[2] * d.vs[2];
+    d.trunc = c->truncation > 0.f ? c->truncation : 1.1f * std::sqrt(dot);
+    d.max_depth = c->max_depth > 0.f ? c->max_depth : 24.0f;
+    d.nx = c->grid[0];
+    d.ny = c->grid[1];
+    d.nz = c->grid[2];
+    return d;
+}
+
+// GPU float->int conversion semantics (cvt.rzi.s32.f32): truncate, saturate,
+// NaN -> 0.  C++'s static_cast is undefined out of range, so spell it out.
+inline int32_t f2i_rz_sat(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483904.0f) return INT32_MIN;
+    return (int32_t)x;
+}
+
+// cvt.rni.s32.f32: round half to even, saturate, NaN -> 0.
+inline int32_t f2i_rn_sat(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483904.0f) return INT32_MIN;
+    return (int32_t)std::nearbyint(x);
+}
+
+// Voxel centre, tsdf_volume.cu:117-119: ((v + 0.5f) * voxel_size) + offset,
+// contracted to one fused multiply-add.
+inline float centre(int64_t v, float vs, float off) {
+    return std::fma((float)v + 0.5f, vs, off);
+}
+
+struct Rot {
+    float r[9];
+};
+
+// se3.cuh:125-140 + 207-223 with the products that feed an add/sub fused.
+Rot compat_rotation(float qx, float qy, float qz, float qw) {
+    const float x = 2 * qx, y = 2 * qy, z = 2 * qz;
+    const float wx = x * qw, wy = y * qw, wz = z * qw;
+    const float xx = x * qx, yy = y * qy, zz = z * qz;
+    Rot R;
+    R.r[0] = 1 - std::fma(y, qy, zz);
+    R.r[1] = std::fma(y, qx, -wz);
+    R.r[2] = std::fma(z, qx, wy);
+    R.r[3] = std::fma(y, qx, wz);
+    R.r[4] = 1 - std::fma(x, qx, zz);
+    R.r[5] = std::fma(z, qy, -wx);
+    R.r[6] = std::fma(z, qx, -wy);
+    R.r[7] = std::fma(z, qy, wx);
+    R.r[8] = 1 - std::fma(x, qx, yy);
+    return R;
+}
+
+// se3.cuh:165-175: rotate then translate; row . p contracted left to right.
+inline float rot_row(const float* r, float px, float py, float pz, float t) {
+    return std::fma(r[2], pz, std::fma(r[0], px, r[1] * py)) + t;
+}
+
+struct CompatPose {
+    Rot R;
+    float t[3];
+};
+
+// tsdf_volume.cu:271-272: quaternion (w,x,y,z) and translation cast to float.
+CompatPose compat_pose(const double* pose) {
+    CompatPose P;
+    P.R = compat_rotation((float)pose[1], (float)pose[2], (float)pose[3], (float)pose[0]);
+    P.t[0] = (float)pose[4];
+    P.t[1] = (float)pose[5];
+    P.t[2] = (float)pose[6];
+    return P;
+}
+
+// camera_util.cu:44-51 then :7-19.  Returns false when the pixel is off the
+// image (tsdf_volume.cu:166).  q_out receives the two pre-truncation values.
+inline void compat_project(const CompatPose& P, const oracle_cfg* c, float px, float py, float pz,
+                           int32_t* u, int32_t* v, float* qu, float* qv, float* cz_out) {
+    *u = 0;
+    *v = 0;
+    *qu = 0.f;
+    *qv = 0.f;
+    *cz_out = 0.f;
+    if (pz == 0.f) return;
+    const float cxv = rot_row(P.R.r + 0, px, py, pz, P.t[0]);
+    const float cyv = rot_row(P.R.r + 3, px, py, pz, P.t[1]);
+    const float czv = rot_row(P.R.r + 6, px, py, pz, P.t[2]);
+    *cz_out = czv;
+    if (czv == 0.f) return;
+    *qu = (cxv * c->fx) / czv + c->cx;
+    *qv = (cyv * c->fy) / czv + c->cy;
+    *u = f2i_rz_sat(*qu);
+    *v = f2i_rz_sat(*qv);
+}
+
+int nthreads(int threads) {
+#ifdef _OPENMP
+    return threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+// Fixed mode projection: P = K [R | t] with R from the normalised quaternion,
+// evaluated in double on the host and rounded to float once.
+struct FixedPose {
+    float P[12];  // rows: fx*R0 + cx*R2 | fy*R1 + cy*R2 | R2 (each 3 + translation)
+};
+
+FixedPose fixed_pose(const double* pose, const oracle_cfg* c) {
+    double qw = pose[0], qx = pose[1], qy = pose[2], qz = pose[3];
+    const double n = std::sqrt(qw * qw + qx * qx + qy * qy + qz * qz);
+    qw /= n;
+    qx /= n;
+    qy /= n;
+    qz /= n;
+    double R[9];
+    R[0] = 1 - 2 * (qy * qy + qz * qz);
+    R[1] = 2 * (qx * qy - qz * qw);
+    R[2] = 2 * (qx * qz + qy * qw);
+    R[3] = 2 * (qx * qy + qz * qw);
+    R[4] = 1 - 2 * (qx * qx + qz * qz);
+    R[5] = 2 * (qy * qz - qx * qw);
+    R[6] = 2 * (qx * qz - qy * qw);
+    R[7] = 2 * (qy * qz + qx * qw);
+    R[8] = 1 - 2 * (qx * qx + qy * qy);
+    const double t[3] = {pose[4], pose[5], pose[6]};
+    const double fx = c->fx, fy = c->fy, cx = c->cx, cy = c->cy;
+    FixedPose F;
+    for (int k = 0; k < 3; ++k) {
+        F.P[0 + k] = (float)(fx * R[0 + k] + cx * R[6 + k]);
+        F.P[4 + k] = (float)(fy * R[3 + k] + cy * R[6 + k]);
+        F.P[8 + k] = (float)R[6 + k];
+    }
+    F.P[3] = (float)(fx * t[0] + cx * t[2]);
+    F.P[7] = (float)(fy * t[1] + cy * t[2]);
+    F.P[11] = (float)t[2];
+    return F;
+}
+
+}  // namespace
+
+extern "C" {
+
+void oracle_derive(const oracle_cfg* c, float* vs_out, float* trunc_out) {
+    Derived d = derive(c);
+    for (int i = 0; i < 3; ++i) vs_out[i] = d.vs[i];
+    *trunc_out = d.trunc;
+}
+
+// tsdf_volume.cu:227-242: weights 0, distances = truncation distance.
+void oracle_volume_init(const oracle_cfg* c, float* D, float* W) {
+    Derived d = derive(c);
+    const int64_t n = d.nx * d.ny * d.nz;
+    for (int64_t i = 0; i < n; ++i) {
+        D[i] = d.trunc;
+        W[i] = 0.f;
+    }
+}
+
+// One frame of cu_tsdf_integrate (tsdf_volume.cu:144-190) in IEEE arithmetic.
+// depth: float metres, rows `pitch_bytes` apart.
+void oracle_integrate_compat(const oracle_cfg* c, float* D, float* W, const float* depth,
+                             int64_t pitch_bytes, int32_t width, int32_t height, const double* pose,
+                             int32_t threads) {
+    const Derived d = derive(c);
+    const CompatPose P = compat_pose(pose);
+    const int64_t rows = d.ny * d.nz;
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (int64_t r = 0; r < rows; ++r) {
+        const int64_t vy = r % d.ny, vz = r / d.ny;
+        const float py = centre(vy, d.vs[1], c->offset[1]);
+        const float pz = centre(vz, d.vs[2], c->offset[2]);
+        int64_t idx = r * d.nx;
+        for (int64_t vx = 0; vx < d.nx; ++vx, ++idx) {
+            const float px = centre(vx, d.vs[0], c->offset[0]);
+            int32_t u, v;
+            float qu, qv, cz;
+            compat_project(P, c, px, py, pz, &u, &v, &qu, &qv, &cz);
+            if (u < 0 || (uint32_t)u >= (uint32_t)width || v < 0 || (uint32_t)v >= (uint32_t)height)
+                continue;
+            const float dv = *(const float*)((const char*)depth + (int64_t)v * pitch_bytes + 4 * (int64_t)u);
+            if (dv <= 0.0f || (double)dv > 24.0) continue;
+            const float sdf = dv - pz;
+            if (sdf >= -d.trunc) {
+                float tsdf = sdf;
+                if (sdf > 0) tsdf = std::fmin(sdf, d.trunc);
+                const float w = W[idx];
+                const float nw = w + 1.0f;
+                const float nd = std::fma(D[idx], w, tsdf) / nw;
+                W[idx] = nw;
+                D[idx] = nd;
+            }
+        }
+    }
+}
+
+// Marks voxels whose compat pixel index could differ between the IEEE
+// arithmetic above and the reference's approximate divide: the value before
+// truncation is within `ulps` float ulps (relative) of a non-zero integer, or
+// a camera/world z is exactly zero.  flags |= 1 for such voxels.
+void oracle_compat_ambiguous(const oracle_cfg* c, const double* pose, int32_t width, int32_t height,
+                             float ulps, uint8_t* flags, int32_t threads) {
+    const Derived d = derive(c);
+    const CompatPose P = compat_pose(pose);
+    const int64_t rows = d.ny * d.nz;
+    (void)width;
+    (void)height;
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (int64_t r = 0; r < rows; ++r) {
+        const int64_t vy = r % d.ny, vz = r / d.ny;
+        const float py = centre(vy, d.vs[1], c->offset[1]);
+        const float pz = centre(vz, d.vs[2], c->offset[2]);
+        int64_t idx = r * d.nx;
+        for (int64_t vx = 0; vx < d.nx; ++vx, ++idx) {
+            const float px = centre(vx, d.vs[0], c->offset[0]);
+            int32_t u, v;
+            float qu, qv, cz;
+            compat_project(P, c, px, py, pz, &u, &v, &qu, &qv, &cz);
+            bool amb = (pz == 0.f) || (cz == 0.f) || std::fabs(cz) < 1e-30f;
+            for (float q : {qu, qv}) {
+                const float rq = std::nearbyint(q);
+                if (rq != 0.f && std::fabs(q - rq) <= ulps * 1.1920929e-7f * std::fmax(1.f, std::fabs(q)))
+                    amb = true;
+            }
+            if (amb) flags[idx] |= 1;
+        }
+    }
+}
+
+// Fixed-mode integrate: camera-space SDF, round-to-nearest pixel, weight clamp.
+// fmt 0: float metres; fmt 1: uint16 scaled by depth_scale.
+void oracle_integrate_fixed(const oracle_cfg* c, float* D, float* W, const void* depth, int64_t pitch_bytes,
+                            int32_t width, int32_t height, int32_t fmt, float depth_scale, const double* pose,
+                            int32_t threads) {
+    const Derived d = derive(c);
+    const FixedPose F = fixed_pose(pose, c);
+    const float* P = F.P;
+    const int64_t rows = d.ny * d.nz;
+    const float wmax = c->max_weight;
+    const float min_z = c->min_z;
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (int64_t r = 0; r < rows; ++r) {
+        const int64_t vy = r % d.ny, vz = r / d.ny;
+        const float py = centre(vy, d.vs[1], c->offset[1]);
+        const float pz = centre(vz, d.vs[2], c->offset[2]);
+        const float aU = std::fma(P[1], py, std::fma(P[2], pz, P[3]));
+        const float aV = std::fma(P[5], py, std::fma(P[6], pz, P[7]));
+        const float aZ = std::fma(P[9], py, std::fma(P[10], pz, P[11]));
+        int64_t idx = r * d.nx;
+        for (int64_t vx = 0; vx < d.nx; ++vx, ++idx) {
+            const float px = centre(vx, d.vs[0], c->offset[0]);
+            const float Z = std::fma(P[8], px, aZ);
+            if (!(Z > min_z)) continue;
+            const float U = std::fma(P[0], px, aU);
+            const float V = std::fma(P[4], px, aV);
+            const float rz = 1.0f / Z;
+            const int32_t u = f2i_rn_sat(U * rz);
+            const int32_t v = f2i_rn_sat(V * rz);
+            if ((uint32_t)u >= (uint32_t)width || (uint32_t)v >= (uint32_t)height) continue;
+            const char* row = (const char*)depth + (int64_t)v * pitch_bytes;
+            float dv;
+            if (fmt == 1)
+                dv = (float)((const uint16_t*)row)[u] * depth_scale;
+            else
+                dv = ((const float*)row)[u];
+            if (!(dv > 0.f && dv <= d.max_depth)) continue;
+            const float sdf = dv - Z;
+            if (!(sdf >= -d.trunc)) continue;
+            const float tsdf = std::fmin(sdf, d.trunc);
+            const float w = W[idx];
+            const int32_t n = std::max(f2i_rz_sat(w), 0);
+            const float inv = 1.0f / (float)(n + 1);
+            D[idx] = std::fma(tsdf - D[idx], inv, D[idx]);
+            W[idx] = std::fmin(w + 1.0f, wmax);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Marching cubes.
+// Corner numbering of marching_cubes.cu:118-127: 0 (x,y,z) 1 (x+1,y,z)
+// 2 (x+1,y,z+1) 3 (x,y,z+1) 4 (x,y+1,z) 5 (x+1,y+1,z) 6 (x+1,y+1,z+1) 7 (x,y+1,z+1)
+// where "z+1" is the next layer.
+static const int kCornerDx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+static const int kCornerDy[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+static const int kCornerDz[8] = {0, 0, 1, 1, 0, 0, 1, 1};
+
+static inline int edge_start(int e) { return GBT_MC_EDGE_ENDS[e] & 15; }
+static inline int edge_end(int e) { return GBT_MC_EDGE_ENDS[e] >> 4; }
+static inline int tri_edge(int type, int k) { return (int)((GBT_MC_TRI_PACKED[type] >> (4 * k)) & 15); }
+
+// Compat mesh: marching_cubes.cu:191-237 with layer stride gx+gy (:211) and
+// positions taken from the voxel at the same linear index (:86-99,216-217).
+// Emits 3 vertices per triangle (:159-189).  verts: 9 floats per triangle,
+// tris: 3 ints per triangle, written only while below cap_tris.  Returns the
+// number of triangles.
+int64_t oracle_mc_compat(const oracle_cfg* c, const float* D, float* verts, int32_t* tris, int64_t cap_tris,
+                         int64_t index_base, int32_t threads) {
+    const Derived d = derive(c);
+    const int64_t gx = d.nx, gy = d.ny, gz = d.nz;
+    if (gx < 2 || gy < 2 || gz < 2) return 0;
+    const int64_t layer = gx + gy;
+    const int64_t nlayers = gz - 1;
+    std::vector<int64_t> counts(nlayers + 1, 0);
+    auto classify = [&](int64_t vz, int64_t vy, int64_t vx, float* val, int64_t* lin) -> int {
+        const int64_t base = vz * layer + vy * gx + vx;
+        const int64_t base2 = base + layer;
+        lin[0] = base;
+        lin[1] = base + 1;
+        lin[2] = base2 + 1;
+        lin[3] = base2;
+        lin[4] = base + gx;
+        lin[5] = base + gx + 1;
+        lin[6] = base2 + gx + 1;
+        lin[7] = base2 + gx;
+        int type = 0;
+        for (int k = 0; k < 8; ++k) {
+            val[k] = D[lin[k]];
+            if (val[k] < 0.f) type |= 1 << k;
+        }
+        return type;
+    };
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(threads))
+    for (int64_t vz = 0; vz < nlayers; ++vz) {
+        int64_t n = 0;
+        for (int64_t vy = 0; vy < gy - 1; ++vy)
+            for (int64_t vx = 0; vx < gx - 1; ++vx) {
+                float val[8];
+                int64_t lin[8];
+                n += GBT_MC_TRI_COUNT[classify(vz, vy, vx, val, lin)];
+            }
+        counts[vz + 1] = n;
+    }
+    for (int64_t i = 0; i < nlayers; ++i) counts[i + 1] += counts[i];
+    const int64_t total = counts[nlayers];
+    const int64_t plane = gx * gy;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(threads))
+    for (int64_t vz = 0; vz < nlayers; ++vz) {
+        int64_t t = counts[vz];
+        for (int64_t vy = 0; vy < gy - 1; ++vy)
+            for (int64_t vx = 0; vx < gx - 1; ++vx) {
+                float val[8];
+                int64_t lin[8];
+                const int type = classify(vz, vy, vx, val, lin);
+                const int ntri = GBT_MC_TRI_COUNT[type];
+                if (!ntri) continue;
+                float pos[8][3];
+                for (int k = 0; k < 8; ++k) {
+                    const int64_t i = lin[k];
+                    pos[k][0] = centre(i % gx, d.vs[0], c->offset[0]);
+                    pos[k][1] = centre((i / gx) % gy, d.vs[1], c->offset[1]);
+                    pos[k][2] = centre(i / plane, d.vs[2], c->offset[2]);
+                }
+                for (int tr = 0; tr < ntri; ++tr, ++t) {
+                    if (t >= cap_tris) continue;
+                    for (int j = 0; j < 3; ++j) {
+                        const int e = tri_edge(type, 3 * tr + j);
+                        int a = edge_start(e), b = edge_end(e);
+                        float s = val[a], en = val[b];
+                        if (s > 0 && en < 0) {  // marching_cubes.cu:34-41
+                            std::swap(a, b);
+                            std::swap(s, en);
+                        }
+                        const float ratio = (-s) / (en - s);
+                        float* out = verts + 9 * t + 3 * j;
+                        for (int k = 0; k < 3; ++k) out[k] = std::fma(ratio, pos[b][k] - pos[a][k], pos[a][k]);
+                        tris[3 * t + j] = (int32_t)(index_base + 3 * t + j);
+                    }
+                }
+            }
+    }
+    return total;
+}
+
+// Fixed-mode mesh: true layer stride, cubes with an unobserved corner
+// (weight 0) skipped, each edge interpolated from its lower-index endpoint so
+// both cubes sharing an edge compute the same point.
+int64_t oracle_mc_fixed(const oracle_cfg* c, const float* D, const float* W, float* verts, int32_t* tris,
+                        int64_t cap_tris, int64_t index_base, int32_t threads) {
+    const Derived d = derive(c);
+    const int64_t gx = d.nx, gy = d.ny, gz = d.nz;
+    if (gx < 2 || gy < 2 || gz < 2) return 0;
+    const int64_t plane = gx * gy;
+    const int64_t nlayers = gz - 1;
+    std::vector<int64_t> counts(nlayers + 1, 0);
+    auto classify = [&](int64_t vz, int64_t vy, int64_t vx, float* val) -> int {
+        int type = 0;
+        for (int k = 0; k < 8; ++k) {
+            const int64_t i = (vz + kCornerDz[k]) * plane + (vy + kCornerDy[k]) * gx + vx + kCornerDx[k];
+            if (!(W[i] > 0.f)) return 0;
+            val[k] = D[i];
+            if (val[k] < 0.f) type |= 1 << k;
+        }
+        return type;
+    };
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(threads))
+    for (int64_t vz = 0; vz < nlayers; ++vz) {
+        int64_t n = 0;
+        for (int64_t vy = 0; vy < gy - 1; ++vy)
+            for (int64_t vx = 0; vx < gx - 1; ++vx) {
+                float val[8];
+                n += GBT_MC_TRI_COUNT[classify(vz, vy, vx, val)];
+            }
+        counts[vz + 1] = n;
+    }
+    for (int64_t i = 0; i < nlayers; ++i) counts[i + 1] += counts[i];
+    const int64_t total = counts[nlayers];
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads(threads))
+    for (int64_t vz = 0; vz < nlayers; ++vz) {
+        int64_t t = counts[vz];
+        for (int64_t vy = 0; vy < gy - 1; ++vy)
+            for (int64_t vx = 0; vx < gx - 1; ++vx) {
+                float val[8];
+                const int type = classify(vz, vy, vx, val);
+                const int ntri = GBT_MC_TRI_COUNT[type];
+                if (!ntri) continue;
+                for (int tr = 0; tr < ntri; ++tr, ++t) {
+                    if (t >= cap_tris) continue;
+                    for (int j = 0; j < 3; ++j) {
+                        const int e = tri_edge(type, 3 * tr + j);
+                        int a = edge_start(e), b = edge_end(e);
+                        // lower endpoint first: the one with the smaller offset on the edge's axis
+                        if (kCornerDx[a] + kCornerDy[a] + kCornerDz[a] > kCornerDx[b] + kCornerDy[b] + kCornerDz[b])
+                            std::swap(a, b);
+                        const float pa[3] = {centre(vx + kCornerDx[a], d.vs[0], c->offset[0]),
+                                             centre(vy + kCornerDy[a], d.vs[1], c->offset[1]),
+                                             centre(vz + kCornerDz[a], d.vs[2], c->offset[2])};
+                        const float pb[3] = {centre(vx + kCornerDx[b], d.vs[0], c->offset[0]),
+                                             centre(vy + kCornerDy[b], d.vs[1], c->offset[1]),
+                                             centre(vz + kCornerDz[b], d.vs[2], c->offset[2])};
+                        const float tt = val[a] / (val[a] - val[b]);
+                        float* out = verts + 9 * t + 3 * j;
+                        for (int k = 0; k < 3; ++k) out[k] = std::fma(tt, pb[k] - pa[k], pa[k]);
+                        tris[3 * t + j] = (int32_t)(index_base + 3 * t + j);
+                    }
+                }
+            }
+    }
+    return total;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+"""Integrate on the GPU against the CPU oracle (through the C ABI)."""
+import numpy as np
+import pytest
+
+from cuphoto import TSDFVolumeConfig
+from cuphoto import synthetic as S
+
+from helpers import circle_case, dev_depth, engine_run, frontal_case, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k", [1, 3, 32])
+@pytest.mark.parametrize("case", ["frontal", "circle", "odd"])
+def test_compat_ieee_bitexact_vs_oracle(gpu, oracle, case, k):
+    """Compat mode in IEEE arithmetic = the oracle's operations: bit-exact,
+    whatever the number of frames fused per pass."""
+    if case == "frontal":
+        seq, tc = frontal_case(frames=7, arith="ieee")
+    elif case == "circle":
+        seq, tc = circle_case(frames=7, arith="ieee")
+    else:  # x not a multiple of 4 (scalar tail path), y/z not multiples of 8
+        seq, tc = frontal_case(77, 50, 37, frames=7, arith="ieee")
+    depths = list(seq.depth_m())
+    _, D, W = engine_run(gpu, tc, depths, seq.poses, k=k)
+    Do, Wo = oracle_run(oracle, tc, depths, seq.poses)
+    assert (Wo > 0).mean() > 0.05
+    assert np.array_equal(W, Wo)
+    assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
+
+
+@pytest.mark.parametrize("fmt", ["u16", "f32"])
+@pytest.mark.parametrize("k", [1, 5, 32])
+@pytest.mark.parametrize("case", ["circle", "odd"])
+def test_fixed_bitexact_vs_oracle(gpu, oracle, case, fmt, k):
+    if case == "circle":
+        seq, tc = circle_case(frames=9, mode="fixed", max_weight=6)
+    else:
+        seq, tc = frontal_case(77, 50, 37, frames=9, mode="fixed", max_weight=6)
+    depths = list(seq.depth_u16) if fmt == "u16" else list(seq.depth_m())
+    _, D, W = engine_run(gpu, tc, depths, seq.poses, k=k)
+    Do, Wo = oracle_run(oracle, tc, depths, seq.poses)
+    assert (Wo > 0).mean() > 0.05 and Wo.max() == 6
+    assert np.array_equal(W, Wo)
+    assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
+
+
+@pytest.mark.parametrize("case", ["frontal", "circle"])
+def test_compat_reference_arith_vs_oracle(gpu, oracle, case):
+    """Compat mode in the reference's arithmetic: weights and distances equal
+    the oracle's except where a pixel index sits within 8 ulp of a truncation
+    boundary; distances elsewhere agree to the approximate divide's error."""
+    seq, tc = (frontal_case if case == "frontal" else circle_case)(frames=7)
+    depths = list(seq.depth_m())
+    _, D, W = engine_run(gpu, tc, depths, seq.poses, k=4)
+    flags = np.zeros(D.shape, np.uint8)
+    Do, Wo = oracle_run(oracle, tc, depths, seq.poses, flags=flags)
+    ok = flags == 0
+    assert ok.mean() > 0.95
+    assert np.array_equal(W[ok], Wo[ok])
+    trunc = oracle.derive(oracle.cfg_from(tc))[1]
+    np.testing.assert_allclose(D[ok], Do[ok], rtol=0, atol=1e-6 * trunc * len(depths))
+    n_flip = int(((W != Wo) | (np.abs(D - Do) > 1e-6 * trunc * len(depths))).sum())
+    assert n_flip <= max(20, 2e-3 * D.size)
+
+
+@pytest.mark.parametrize("mode", ["compat", "fixed"])
+@pytest.mark.parametrize("brick", [0, 1, 2, 3])
+def test_fused_pass_equals_per_frame_passes(gpu, mode, brick):
+    """Frames fused in one pass give bit-identical volumes to one pass per
+    frame, for every brick shape (full-size-independent property)."""
+    seq, tc = circle_case(n=96, frames=16, mode=mode, max_weight=8)
+    depths = list(seq.depth_u16) if mode == "fixed" else list(seq.depth_m())
+    _, D1, W1 = engine_run(gpu, tc, depths, seq.poses, k=1, brick=brick)
+    _, D2, W2 = engine_run(gpu, tc, depths, seq.poses, k=16, brick=brick, ctas_per_sm=3)
+    assert np.array_equal(W1, W2) and np.array_equal(D1.view(np.uint32), D2.view(np.uint32))
+
+
+def test_edge_cases_invalid_depth(gpu, oracle):
+    """Zero, NaN, negative and beyond-range depth are skipped; a pitched
+    image (row stride above width) is read through its pitch."""
+    seq, tc = frontal_case(64, 48, 32, frames=2, arith="ieee")
+    d = seq.depth_m()[0].copy()
+    h, w = d.shape
+    d[:, : w // 4] = 0.0
+    d[: h // 4, :] = np.nan
+    d[h // 2:, w // 2:] = 30.0      # beyond the reference's 24 m limit
+    d[h // 3: h // 2, :] = -1.0
+    pitched = np.zeros((h, w + 13), np.float32)
+    pitched[:, :w] = d
+    t = gpu.from_numpy(pitched).cuda()[:, :w]
+    from cuphoto import TSDFVolume
+    vol = TSDFVolume(tc)
+    assert vol.integrate(t, t, seq.poses[0])
+    gpu.cuda.synchronize()
+    Do, Wo = oracle_run(oracle, tc, [d], seq.poses[:1])
+    assert np.array_equal(vol.voxel_weights_data().cpu().numpy(), Wo)
+    assert np.array_equal(vol.voxel_distances_data().cpu().numpy(), Do)
+
+
+def test_reference_error_behaviour(gpu):
+    """integrate() returns False for missing or empty images, as the reference does."""
+    from cuphoto import TSDFVolume
+    seq, tc = frontal_case(16, 16, 16, frames=1)
+    vol = TSDFVolume(tc)
+    d = dev_depth(gpu, seq.depth_m()[0])
+    assert vol.integrate(None, d, seq.poses[0]) is False
+    assert vol.integrate(d, None, seq.poses[0]) is False
+    assert vol.integrate(d, d[:0], seq.poses[0]) is False
+    bad_pose = np.array(seq.poses[0]).copy()
+    bad_pose[4] = np.nan
+    assert vol.integrate(d, d, bad_pose) is False
+    W = vol.voxel_weights_data().cpu().numpy()
+    assert np.all(W == 0)
+
+
+def test_camera_facing_away_leaves_volume_untouched(gpu):
+    seq, tc = circle_case(n=48, frames=1, mode="fixed")
+    pose = S.pose7(*S.look_at((0.0, 0.5, 5.0), target=(0.0, 0.5, 10.0)))
+    _, D, W = engine_run(gpu, tc, [seq.depth_u16[0]], [pose])
+    assert np.all(W == 0)
+
+
+@pytest.mark.parametrize("mode", ["compat", "fixed"])
+def test_full_size_c1_against_oracle(gpu, oracle, mode):
+    """256^3 grid, 20 frames of 640x480 (the 1 cm configuration), fused 20 per
+    pass, against the oracle: bit-exact in IEEE/fixed arithmetic."""
+    cam = S.Camera()
+    seq = S.make_sequence(20, scene_id=0, camera=cam, trajectory="circle")
+    kw = dict(arith="ieee") if mode == "compat" else dict(mode="fixed", max_weight=128)
+    tc = TSDFVolumeConfig(**S.grid_for(256), **kw)
+    depths = list(seq.depth_m()) if mode == "compat" else list(seq.depth_u16)
+    _, D, W = engine_run(gpu, tc, depths, seq.poses, k=20)
+    Do, Wo = oracle_run(oracle, tc, depths, seq.poses)
+    assert np.array_equal(W, Wo)
+    assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
