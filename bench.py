@@ -1,0 +1,404 @@
+"""Benchmark of the TSDF engine: batched integrate + marching cubes.
+
+Workload (the batched plain-forward configuration): a 512^3 grid of 0.5 cm
+voxels (2.56 m cube, FP32 distance + FP32 weight = 1 GiB), 300 synthetic
+640x480 uint16 depth frames along a helix around a seeded plane+spheres scene,
+fx=fy=525, cx=319.5, cy=239.5, integrated K frames per pass (K, brick shape
+and CTAs/SM chosen by the autotuner) inside a captured CUDA graph, then the
+iso-0 mesh extracted.  One step = reset the volume, integrate all 300 frames,
+extract the mesh.  Metric: voxel-updates/s = 512^3 * 300 per step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mode compat|fixed]
+
+With torchrun (N > 1) every rank runs its own scene (seed = rank) on its own
+GPU: independent volumes, weak scaling, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cu-reconstruction_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "TSDF voxel-updates/s & %HBM peak; fwd+adjoint vs plain fwd time, 1 GB300"
+UNIT = "voxel-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="compat", choices=["compat", "fixed"])
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--frames", type=int, default=300)
+    ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
+    ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload(args, rank):
+    from cuphoto import synthetic as S
+    cam = S.Camera()
+    scene = S.make_scene(scene_id=rank, n_spheres=6)
+    poses = S.helix_poses(args.frames, seed=rank)
+    return S, cam, scene, poses
+
+
+def volume_cfg(args, cam, mode):
+    from cuphoto import TSDFVolumeConfig
+    from cuphoto import synthetic as S
+    return TSDFVolumeConfig(**S.grid_for(args.grid, 2.56), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy,
+                            camera_width=cam.width, camera_height=cam.height, max_weight=128.0, mode=mode)
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx = max(mx, float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(args, cam, scene, poses, budget_s=12.0):
+    """The oracle's OpenMP restatement of the reference integrate on the host
+    cores, on the full grid, for as many frames as fit in `budget_s`."""
+    import oracle
+    from cuphoto import synthetic as S
+    oracle.ensure_built()
+    tc = volume_cfg(args, cam, "compat")
+    c = oracle.cfg_from(tc)
+    D, W = oracle.init_volume(c)
+    cores = os.cpu_count() or 1
+    nvox = args.grid ** 3
+    done, spent = 0, 0.0
+    for k, p in enumerate(poses):
+        dm = S.u16_to_metres(S.render_depth_u16(scene, p, cam, frame_seed=k))   # rendering is not timed
+        a = time.perf_counter()
+        oracle.integrate_compat(c, D, W, dm, p, threads=cores)
+        spent += time.perf_counter() - a
+        done += 1
+        if spent > budget_s:
+            break
+    return {"value": nvox * done / spent, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d frames integrated into the full %d^3 grid (compat arithmetic, OpenMP over rows)"
+                      % (done, len(poses), args.grid), "seconds": spent}
+
+
+def reference_cuda(args, cam, scene, poses, torch, nframes=8):
+    """The reference's own integrate kernel (built from its sources) on this GPU."""
+    import oracle
+    if not oracle.RefHarness.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref/ref_tsdf.cubin missing)"}
+    from cuphoto import synthetic as S
+    tc = volume_cfg(args, cam, "compat")
+    r = oracle.RefHarness(tc)
+    ms = []
+    for k in range(nframes):
+        d = torch.from_numpy(S.u16_to_metres(S.render_depth_u16(scene, poses[k], cam, frame_seed=k))).cuda()
+        t0 = time.perf_counter()
+        kms = r.integrate(d.data_ptr(), d.stride(0) * 4, d.shape[1], d.shape[0], poses[k])
+        wall = time.perf_counter() - t0
+        if k > 0:  # first frame warms up
+            ms.append((kms, wall * 1e3))
+    r.close()
+    nvox = args.grid ** 3
+    kern = float(np.median([m[0] for m in ms]))
+    wall = float(np.median([m[1] for m in ms]))
+    return {"value": nvox / (kern * 1e-3), "unit": UNIT, "kernel_ms_per_frame": kern, "call_ms_per_frame": wall,
+            "frames_timed": len(ms), "what": "TSDFVolume::integrate of the reference, one launch + sync per frame"}
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    S, cam, scene, poses = workload(args, 0)
+    import oracle
+    from cuphoto import synthetic as SS
+    oracle.ensure_built()
+    tc = volume_cfg(args, cam, "compat")
+    c = oracle.cfg_from(tc)
+    D, W = oracle.init_volume(c)
+    cores = os.cpu_count() or 1
+    frames = [SS.u16_to_metres(SS.render_depth_u16(scene, p, cam, frame_seed=k)) for k, p in enumerate(poses[:4])]
+    nvox = args.grid ** 3
+    # each step integrates a bounded sample of the frames (sized to ~4 s of host time)
+    t = time.perf_counter()
+    oracle.integrate_compat(c, D, W, frames[0], poses[0], threads=cores)
+    per_frame = time.perf_counter() - t
+    fps = max(1, min(4, int(4.0 / max(per_frame, 1e-3))))
+    for _ in range(args.warmup):
+        for k in range(fps):
+            oracle.integrate_compat(c, D, W, frames[k % 4], poses[k % 4], threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        for k in range(fps):
+            oracle.integrate_compat(c, D, W, frames[k % 4], poses[k % 4], threads=cores)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = nvox * fps * args.steps / total
+    sample = "%d frames per step into the full %d^3 grid (compat arithmetic, OpenMP over rows)" % (fps, args.grid)
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "batched integrate, %d^3 voxels of 0.5 cm, 640x480 uint16 depth (CPU sample)" % args.grid,
+                      "grid": args.grid, "frames_per_step": fps},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+    eb = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(eb)
+    if rank == 0:
+        eb.build()
+    if world > 1:
+        torch.distributed.barrier()
+    import ctypes as C
+    from cuphoto import TSDFVolume, extract_mesh_device, make_frame
+    from cuphoto import _lib as L
+    from cuphoto.autotune import tune_integrate
+
+    S, cam, scene, poses = workload(args, rank)
+    nf = len(poses)
+    nvox = args.grid ** 3
+    frames_dev = S.render_sequence_torch(scene, poses, cam, seed=rank)          # (n, H, W) int16 = u16 bits
+    frames_host = torch.empty(frames_dev.shape, dtype=torch.int16, pin_memory=True)
+    frames_host.copy_(frames_dev)
+    torch.cuda.synchronize()
+    tc = volume_cfg(args, cam, args.mode)
+    vol = TSDFVolume(tc)
+    depths = [frames_dev[k] for k in range(nf)]
+
+    if args.config:
+        b_, k_, c_ = (int(x) for x in args.config.split(","))
+        tune = {"brick": b_, "frames": k_, "ctas": c_, "ns_per_update": None, "table": []}
+    else:
+        tune = tune_integrate(vol, depths, poses)
+    K, brick, ctas = tune["frames"], tune["brick"], tune["ctas"]
+    n_passes = (nf + K - 1) // K
+
+    # mesh capacity from an untimed run
+    vol.reset()
+    vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+    V0, T0 = extract_mesh_device(vol)
+    cap = max(1024, int(len(V0) * 1.25) + 1024)
+    verts = torch.empty((cap, 3, 3), dtype=torch.float32, device="cuda")
+    tris = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    lib = L.lib()
+
+    def step_reset():
+        vol.reset()
+
+    def step_integrate():
+        vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+
+    def step_mesh():
+        L.check(lib.gbt_extract_mesh_async(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
+                                           cap, 0, C.c_void_p(count.data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+    stream = torch.cuda.Stream()
+    graphs = []
+    with torch.cuda.stream(stream):
+        for fn in (step_reset, step_integrate, step_mesh):   # warm the path once outside capture
+            fn()
+        torch.cuda.synchronize()
+        for fn in (step_reset, step_integrate, step_mesh):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                fn()
+            graphs.append(g)
+    g_reset, g_int, g_mesh = graphs
+
+    for _ in range(args.warmup):
+        for g in graphs:
+            g.replay()
+    torch.cuda.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            g_reset.replay()
+            ev[i][1].record(stream)
+            g_int.replay()
+            ev[i][2].record(stream)
+            g_mesh.replay()
+            ev[i][3].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [ev[i][0].elapsed_time(ev[i][3]) for i in range(args.steps)]
+    int_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
+    mesh_ms = [ev[i][2].elapsed_time(ev[i][3]) for i in range(args.steps)]
+    total_ms = ev[0][0].elapsed_time(ev[-1][3])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ntri = int(count.item())
+    value = world * nvox * nf * args.steps / (total_ms * 1e-3)
+
+    # roofline of the dominant kernel (the integrate pass), from the timed region
+    launch_ms = float(np.mean(int_ms)) / n_passes
+    frame_px = cam.width * cam.height
+    alg_bytes = 16.0 * nvox + (nf / n_passes) * frame_px * 2 + (nf / n_passes) * 64
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    # end to end through the public API with host buffers: H2D of the step's
+    # depth frames from pinned memory, integrate, mesh, D2H of the mesh
+    e2e_ms = []
+    h2d = frames_host.numel() * 2
+    d2h = 0
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        frames_dev.copy_(frames_host, non_blocking=True)
+        vol.reset()
+        vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+        V, T = extract_mesh_device(vol, capacity=cap)
+        Vh = V.cpu()
+        Th = T.cpu()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            d2h = Vh.numel() * 4 + Th.numel() * 4 + 8
+    e2e_value = world * nvox * nf / (float(np.mean(e2e_ms)) * 1e-3)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    extras = {}
+    if not args.no_extras and world == 1:
+        extras["reference_cuda"] = reference_cuda(args, cam, scene, poses, torch)
+        cpu = cpu_baseline(args, cam, scene, poses)
+    else:
+        cpu = None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: seeded plane + 6 spheres, ray-cast uint16 depth, helix trajectory",
+        "config": {"workload": "batched integrate + marching cubes, %d^3 voxels of 0.5 cm, %d frames 640x480 uint16"
+                               % (args.grid, nf),
+                   "mode": args.mode, "frames_per_pass": K, "brick": brick, "ctas_per_sm": ctas,
+                   "passes_per_step": n_passes, "graph": "reset, integrate passes, mesh captured as CUDA graphs",
+                   "l2": "inputs larger than L2: 1 GiB volume + %d MB depth per step" % (frames_dev.numel() * 2 // 2**20),
+                   "triangles": ntri},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "integrate_kernel", "launch_ms": launch_ms,
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind},
+        "breakdown_ms": {"reset": float(np.mean([ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)])),
+                         "integrate": float(np.mean(int_ms)), "mesh": float(np.mean(mesh_ms))},
+        "integrate_only": {"value": nvox * nf / (float(np.mean(int_ms)) * 1e-3), "unit": UNIT},
+        "mesh": {"triangles_per_s": ntri / (float(np.mean(mesh_ms)) * 1e-3) if ntri else 0.0, "triangles": ntri},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": float(np.mean(e2e_ms))},
+        "gpu_launches": args.steps * (1 + n_passes + 1),
+        "clocks": clocks.summary(),
+        "wall_s_timed": t_wall,
+        "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": len(tune["table"])},
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    out.update(extras)
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

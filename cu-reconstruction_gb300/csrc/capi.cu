@@ -294,8 +294,6 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
         fd.t[1] = (float)f.pose[5];
         fd.t[2] = (float)f.pose[6];
         if (v->cfg.mode == GBT_MODE_FIXED) fixed_projection(f.pose, v->cfg, fd.P);
-        if (v->cfg.mode == GBT_MODE_COMPAT && f.format != GBT_DEPTH_F32_M)
-            return fail(GBT_ERR_INVALID_ARG, "compat mode takes float depth in metres (frame %d)", i);
     }
     int bx, by, bz;
     gbt::brick_extent(brick, &bx, &by, &bz);

@@ -14,12 +14,19 @@
 
 #include "gbt_internal.h"
 
+#ifndef GBT_ARITH_NS
+#error "define GBT_ARITH_NS (one namespace per arithmetic translation unit)"
+#endif
+
 #define GBT_MC_CONST static __constant__
 #include "mc_tables.inc"
 GBT_MC_TABLE_DATA
 #undef GBT_MC_CONST
 
 namespace gbt {
+// The kernels below are compiled once per arithmetic; each translation unit
+// puts them in its own namespace so the two sets never share a symbol.
+namespace GBT_ARITH_NS {
 
 enum { kCompat = 0, kFixed = 1 };
 
@@ -89,6 +96,10 @@ __device__ __forceinline__ float mc_ratio(float s, float e) { return __fdiv_rn(-
 __device__ __forceinline__ float mc_lerp(float a, float b, float r) { return __fmaf_rn(r, __fsub_rn(b, a), a); }
 
 #endif
+
+__device__ __forceinline__ float u16_metres(unsigned short raw, float scale) {
+    return __fmul_rn((float)raw, scale);
+}
 
 __device__ __forceinline__ uint32_t fastdiv(uint32_t n, const FastDiv& f) {
     if (f.d == 1) return n;
@@ -290,7 +301,12 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
                     }
                     // tsdf_volume.cu:166-187
                     if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
-                    const float dv = __ldg(reinterpret_cast<const float*>(dimg + (int64_t)vv * pitch) + u);
+                    const char* row = dimg + (int64_t)vv * pitch;
+                    // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
+                    // (rgbd_dataset.cpp:29): one float multiply
+                    const float dv = fd.fmt == GBT_DEPTH_U16
+                                         ? u16_metres(__ldg(reinterpret_cast<const unsigned short*>(row) + u), fd.scale)
+                                         : __ldg(reinterpret_cast<const float*>(row) + u);
                     if (dv <= 0.0f || dv > 24.0) continue;
                     const float sdf = dv - pz;
                     if (sdf >= -v.trunc) {
@@ -602,4 +618,5 @@ cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+}  // namespace GBT_ARITH_NS
 }  // namespace gbt

@@ -3,14 +3,17 @@
 // built with (modules/CMakeLists.txt:17-22), so that its divisions and
 // multiply-add contractions come out as the reference's do.
 #define GBT_REF_ARITH 1
+#define GBT_ARITH_NS refarith
 #include "gbt_kernels.cuh"
 
 namespace gbt {
 
 cudaError_t launch_integrate_compat_ref(const IntegrateArgs& a, int brick, int grid, cudaStream_t s) {
-    return launch_integrate_mode<kCompat>(a, brick, grid, s);
+    return refarith::launch_integrate_mode<refarith::kCompat>(a, brick, grid, s);
 }
 
-cudaError_t launch_mc_compat_ref(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kCompat>(a, s); }
+cudaError_t launch_mc_compat_ref(const McArgs& a, cudaStream_t s) {
+    return refarith::launch_mc_mode<refarith::kCompat>(a, s);
+}
 
 }  // namespace gbt

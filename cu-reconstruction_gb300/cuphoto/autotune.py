@@ -1,0 +1,85 @@
+"""Autotuner for the integrate pass: brick shape x frames per pass x CTAs per SM.
+
+Each candidate integrates the same frames into the volume (which is reset
+before and after), timed with CUDA events on the launching stream; the
+fastest is kept.  Results are cached per (GPU, grid, image size, mode,
+arithmetic) in a JSON file next to the engine library.
+"""
+import json
+import os
+
+from . import _lib as L
+
+BRICKS = (0, 1, 2, 3)
+FRAMES = (8, 16, 32)
+CTAS = (4, 8, 12, 16)
+CACHE = os.path.join(L.PKG_ROOT, "_build", "autotune.json")
+
+
+def _key(vol, width, height):
+    import torch
+    c = vol.cfg
+    return "%s|%s|%dx%d|%s|%s" % (torch.cuda.get_device_name(), "x".join(map(str, c.voxel_grid_size)), width, height,
+                                  c.mode, c.arith)
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _store(d):
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        tmp = CACHE + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def tune_integrate(vol, depths, poses, depth_scale=0.001, bricks=BRICKS, frames=FRAMES, ctas=CTAS, repeats=2,
+                   use_cache=True):
+    """Returns {"brick", "frames", "ctas", "ns_per_update", "table"} for this volume and frame size."""
+    import torch
+    h, w = int(depths[0].shape[0]), int(depths[0].shape[1])
+    key = _key(vol, w, h)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        return cache[key]
+    nvox = 1
+    for g in vol.voxel_grid_size():
+        nvox *= g
+    table = []
+    best = None
+    stream = torch.cuda.current_stream()
+    for k in frames:
+        n = min(len(depths), 2 * k)
+        for b in bricks:
+            for c in ctas:
+                vol.reset()
+                vol.integrate_sequence(depths[:n], poses[:n], frames_per_pass=k, depth_scale=depth_scale, brick=b,
+                                       ctas_per_sm=c)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(repeats):
+                    vol.integrate_sequence(depths[:n], poses[:n], frames_per_pass=k, depth_scale=depth_scale,
+                                           brick=b, ctas_per_sm=c)
+                e1.record(stream)
+                e1.synchronize()
+                ns = e0.elapsed_time(e1) * 1e6 / (repeats * n * nvox)
+                table.append((b, k, c, ns))
+                if best is None or ns < best[3]:
+                    best = (b, k, c, ns)
+    vol.reset()
+    torch.cuda.synchronize()
+    res = {"brick": best[0], "frames": best[1], "ctas": best[2], "ns_per_update": best[3], "table": table}
+    if use_cache:
+        cache[key] = res
+        _store(cache)
+    return res

@@ -258,3 +258,46 @@ def frontal_grid(nx, ny, nz, physical=(2.0, 1.6, 2.56), z0=0.5):
     """Grid in front of the identity camera, starting at depth z0."""
     return dict(voxel_grid_size=(nx, ny, nz), physical_size=tuple(physical),
                 global_offset=(-physical[0] / 2, -physical[1] / 2, z0))
+
+
+def render_sequence_torch(scene, poses, cam, seed=0, sigma=0.001, drop=0.02, depth_scale=0.001, max_range=8.0,
+                          device="cuda"):
+    """The same ray-cast as render_depth_u16, batched on the GPU with torch
+    (float64 geometry, noise from a seeded torch generator).  Returns an
+    (n, H, W) int16 tensor holding the uint16 depth bits, on `device`."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    u = torch.arange(cam.width, dtype=torch.float64, device=device)
+    v = torch.arange(cam.height, dtype=torch.float64, device=device)
+    vv, uu = torch.meshgrid(v, u, indexing="ij")
+    dc = torch.stack([(uu - cam.cx) / cam.fx, (vv - cam.cy) / cam.fy, torch.ones_like(uu)], -1)
+    centres = torch.tensor(scene.centres, dtype=torch.float64, device=device)
+    radii = torch.tensor(scene.radii, dtype=torch.float64, device=device)
+    out = torch.empty((len(poses), cam.height, cam.width), dtype=torch.int16, device=device)
+    for k, pose in enumerate(poses):
+        R = torch.tensor(matrix_from_quat(np.asarray(pose[:4], np.float64)), dtype=torch.float64, device=device)
+        t = torch.tensor(np.asarray(pose[4:], np.float64), dtype=torch.float64, device=device)
+        C = -R.T @ t
+        dw = dc @ R
+        best = torch.full(uu.shape, float("inf"), dtype=torch.float64, device=device)
+        tp = (scene.plane_y - C[1]) / dw[..., 1]
+        best = torch.where((tp > 1e-6) & (tp < best), tp, best)
+        a = (dw * dw).sum(-1)
+        for c, r in zip(centres, radii):
+            oc = C - c
+            b = dw @ oc
+            cc = oc @ oc - r * r
+            disc = b * b - a * cc
+            ok = disc >= 0
+            sq = torch.sqrt(torch.clamp(disc, min=0.0))
+            t0 = (-b - sq) / a
+            t1 = (-b + sq) / a
+            tt = torch.where(t0 > 1e-6, t0, t1)
+            best = torch.where(ok & (tt > 1e-6) & (tt < best), tt, best)
+        z = best + sigma * torch.randn(best.shape, generator=gen, dtype=torch.float64, device=device)
+        raw = torch.where(torch.isfinite(z) & (z < max_range), torch.round(z / depth_scale), torch.zeros_like(z))
+        raw = torch.clamp(raw, 0, 65535)
+        raw = torch.where(torch.rand(raw.shape, generator=gen, device=device) < drop, torch.zeros_like(raw), raw)
+        out[k] = (raw.to(torch.int32) - (raw >= 32768).to(torch.int32) * 65536).to(torch.int16)
+    return out

@@ -312,14 +312,19 @@ def test_oracle_against_reference_golden(oracle, path):
         oracle.integrate_compat(c, D, W, depth[k], g["poses"][k])
         oracle.compat_ambiguous(c, g["poses"][k], w, h, 8.0, flags)
     Dr, Wr = g["D"], g["W"]
-    diff = (D != Dr) | (W != Wr)
-    assert np.all(np.abs(W - Wr)[diff & (flags == 0)] == 0)
-    # away from ambiguous pixels the distances agree to the reference's division error
     ok = flags == 0
-    np.testing.assert_allclose(D[ok], Dr[ok], rtol=0, atol=4e-6 * float(oracle.derive(c)[1]) * len(depth) + 1e-9)
-    assert (diff & ~ok).sum() <= max(10, 1e-3 * D.size)
+    trunc = float(oracle.derive(c)[1])
+    tol = 1e-6 * trunc * len(depth)
+    # weights differ only where a pixel index is ambiguous
+    assert np.all(W[ok] == Wr[ok])
+    # away from ambiguous pixels the distances agree to the reference's division error
+    np.testing.assert_allclose(D[ok], Dr[ok], rtol=0, atol=tol)
+    # and the ambiguous voxels that did flip to another pixel are few
+    flipped = (~ok) & ((W != Wr) | (np.abs(D - Dr) > tol))
+    assert flipped.sum() <= max(10, 1e-3 * D.size)
     # mesh of the reference's own field
     V, T = oracle.mc_compat(c, Dr.ravel())
     assert len(V) == int(g["ntri"])
-    np.testing.assert_allclose(V, g["verts"], rtol=0, atol=1e-5 * float(np.max(oracle.derive(c)[0])))
+    tol = max(1e-5 * float(np.max(oracle.derive(c)[0])), 2 * float(np.spacing(np.float32(np.abs(V).max(initial=1)))))
+    np.testing.assert_allclose(V, g["verts"], rtol=0, atol=tol)
     assert np.array_equal(T, g["tris"])
