@@ -297,6 +297,8 @@ def main():
             graphs.append(g)
     g_reset, g_int, g_mesh = graphs
 
+    # graphs replay on the current stream: make it the stream the events go on
+    torch.cuda.set_stream(stream)
     for _ in range(args.warmup):
         for g in graphs:
             g.replay()

@@ -90,6 +90,14 @@ int ref_load(const char* cubin_path, const char* names_path) {
 
 int ref_volume_create(const uint32_t* grid, const float* phys, const float* offset, float max_weight, float fx,
                       float fy, float cx, float cy, ref_volume** out) {
+    // The reference's integrate kernel guards its (y, z) threads with
+    // `vy >= gy && vz >= gz` (tsdf_volume.cu:154): with y or z not a multiple
+    // of its 8x8 block, threads past the grid run and access out of bounds.
+    // Such grids are refused here, before anything reaches the GPU.
+    if (grid[1] % 8 != 0 || grid[2] % 8 != 0 || grid[0] < 2 || grid[1] < 2 || grid[2] < 2) {
+        g_err = "reference kernels need y and z grid sizes that are multiples of 8 (and every size >= 2)";
+        return 1;
+    }
     ref_volume* v = new ref_volume();
     v->grid = dim3(grid[0], grid[1], grid[2]);
     v->phys = make_float3(phys[0], phys[1], phys[2]);

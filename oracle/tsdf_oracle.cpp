@@ -107,13 +107,15 @@ struct Rot {
     float r[9];
 };
 
-// se3.cuh:125-140 + 207-223 with the products that feed an add/sub fused.
+// se3.cuh:125-140 + 207-223 in the rounding order of the reference's build:
+// the first product of each entry fused into the add/sub, except
+// R00 = 1-(yy+zz), which rounds both products.
 Rot compat_rotation(float qx, float qy, float qz, float qw) {
     const float x = 2 * qx, y = 2 * qy, z = 2 * qz;
     const float wx = x * qw, wy = y * qw, wz = z * qw;
     const float xx = x * qx, yy = y * qy, zz = z * qz;
     Rot R;
-    R.r[0] = 1 - std::fma(y, qy, zz);
+    R.r[0] = 1 - (yy + zz);
     R.r[1] = std::fma(y, qx, -wz);
     R.r[2] = std::fma(z, qx, wy);
     R.r[3] = std::fma(y, qx, wz);
