@@ -25,6 +25,7 @@ UNITS = {
     "k_ieee.cu": [],
     "k_util.cu": [],
     "capi.cu": [],
+    "k_noalloc.cu": [],
 }
 
 

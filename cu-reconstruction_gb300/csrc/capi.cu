@@ -56,6 +56,11 @@ struct gbt_volume {
 
 namespace gbt {
 
+const VolDesc* volume_desc(const gbt_volume* v) { return &v->desc; }
+int volume_mode(const gbt_volume* v) { return v->cfg.mode; }
+int volume_arith(const gbt_volume* v) { return v->cfg.arith; }
+void set_last_error(const char* msg) { g_last_error = msg; }
+
 int integrate_default_ctas_per_sm() { return 8; }
 
 void brick_extent(int brick, int* bx, int* by, int* bz) {

@@ -105,6 +105,13 @@ cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s);
 cudaError_t launch_volume_init(float* D, float* W, int64_t n, float trunc, cudaStream_t s);
 cudaError_t launch_tvoxels(void* out, const VolDesc& v, cudaStream_t s);
 
+// Read-only views of a volume for translation units other than capi.cu.
+const VolDesc* volume_desc(const gbt_volume* v);
+int volume_mode(const gbt_volume* v);
+int volume_arith(const gbt_volume* v);
+// Sets the message gbt_last_error() returns on this thread.
+void set_last_error(const char* msg);
+
 // CTAs per SM the integrate launchers use by default, and brick extents.
 int integrate_default_ctas_per_sm();
 void brick_extent(int brick, int* bx, int* by, int* bz);

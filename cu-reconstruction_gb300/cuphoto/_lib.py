@@ -86,6 +86,8 @@ SIGNATURES = [
                                    C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                          C.c_void_p, C.c_void_p]),
+    ("gbt_extract_mesh_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                           C.c_void_p, C.c_void_p]),
     ("gbt_last_error", C.c_char_p, []),
     ("gbt_version", C.c_char_p, []),
 ]
