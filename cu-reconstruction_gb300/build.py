@@ -58,8 +58,45 @@ def _compile(unit, extra, verbose):
     return obj, r.stderr
 
 
+CPP = os.path.join(HERE, "cpp")
+SHIM = os.path.join(OUT_DIR, "libcuphoto_gb300.so")
+EXAMPLE = os.path.join(OUT_DIR, "tsdf_surface_headless")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def build_cpp(force=False):
+    """The C++ layer over the C ABI (cuphoto::TSDFVolume, TSDFSurface, Mesh,
+    Config) and the headless example driver."""
+    srcs = sorted(os.path.join(CPP, "src", f) for f in os.listdir(os.path.join(CPP, "src")) if f.endswith(".cpp"))
+    hdrs = sorted(os.path.join(CPP, "include", "cuphoto", f) for f in os.listdir(os.path.join(CPP, "include", "cuphoto")))
+    ex = os.path.join(CPP, "examples", "tsdf_surface_headless.cpp")
+    inc = ["-I" + os.path.join(CPP, "include"), "-I" + os.path.join(HERE, "..", "include"),
+           "-I" + os.path.join(CUDA_HOME, "include")]
+    libs = ["-L" + OUT_DIR, "-lgbt_tsdf", "-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart",
+            "-Wl,-rpath," + OUT_DIR, "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
+    flags = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off"]
+    if force or _stale(SHIM, srcs + hdrs + [LIB]):
+        r = subprocess.run(flags + ["-shared"] + inc + srcs + ["-o", SHIM + ".tmp"] + libs, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("C++ layer build failed:\n%s" % r.stderr[-4000:])
+        os.replace(SHIM + ".tmp", SHIM)
+    if force or _stale(EXAMPLE, [ex, SHIM] + hdrs):
+        r = subprocess.run(flags + inc + [ex, "-o", EXAMPLE + ".tmp", "-L" + OUT_DIR, "-lcuphoto_gb300"] + libs,
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("example build failed:\n%s" % r.stderr[-4000:])
+        os.replace(EXAMPLE + ".tmp", EXAMPLE)
+    return SHIM, EXAMPLE
+
+
 def build(force=False, verbose=False):
     """Compile every translation unit and link the shared library; returns its path."""
+    lib = build_engine(force, verbose)
+    build_cpp(force)
+    return lib
+
+
+def build_engine(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     deps = _sources() + [os.path.join(HERE, "..", "include", "gbt_tsdf.h"), os.path.abspath(__file__)]
     if not force and not _stale(LIB, deps):

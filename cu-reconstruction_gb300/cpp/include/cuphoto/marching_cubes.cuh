@@ -1,0 +1,21 @@
+// cuphoto::generate_triangular_surface on the GB300 engine
+// (reference: modules/include/cuda/marching_cubes.cuh:13-15).  Appends to the
+// caller's vectors: three vertices per triangle, indices offset by the
+// vertices already present, in the reference's order.
+#ifndef CUPHOTO_GB300_MARCHING_CUBES_CUH
+#define CUPHOTO_GB300_MARCHING_CUBES_CUH
+
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "tsdf_volume.cuh"
+
+namespace cuphoto {
+
+void generate_triangular_surface(const TSDFVolume& tsdf_volume, std::vector<float3>& verts,
+                                 std::vector<int3>& triangles);
+
+}  // namespace cuphoto
+
+#endif

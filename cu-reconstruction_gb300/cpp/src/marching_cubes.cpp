@@ -1,0 +1,46 @@
+// generate_triangular_surface over the engine's C ABI
+// (reference: marching_cubes.cu:159-237).
+#include "cuphoto/marching_cubes.cuh"
+
+#include <cstdio>
+
+namespace cuphoto {
+
+void generate_triangular_surface(const TSDFVolume& tsdf_volume, std::vector<float3>& vertices,
+                                 std::vector<int3>& triangles) {
+    gbt_volume* vol = tsdf_volume.engine();
+    if (!vol) {
+        std::fprintf(stderr, "[cuda]   generate_triangular_surface() -- volume was not allocated\n");
+        return;
+    }
+    int64_t n = 0;
+    if (gbt_extract_mesh(vol, nullptr, nullptr, 0, 0, &n, nullptr) != GBT_OK) {
+        std::fprintf(stderr, "[cuda]   generate_triangular_surface() -- %s\n", gbt_last_error());
+        return;
+    }
+    if (n == 0) return;
+    float* d_verts = nullptr;
+    int32_t* d_tris = nullptr;
+    if (cudaMalloc(&d_verts, (size_t)n * 9 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&d_tris, (size_t)n * 3 * sizeof(int32_t)) != cudaSuccess) {
+        std::fprintf(stderr, "[cuda]   generate_triangular_surface() -- failed to allocate the mesh buffers\n");
+        cudaFree(d_verts);
+        cudaFree(d_tris);
+        return;
+    }
+    const int64_t base = (int64_t)vertices.size();
+    int64_t n2 = 0;
+    if (gbt_extract_mesh(vol, d_verts, d_tris, n, base, &n2, nullptr) != GBT_OK) {
+        std::fprintf(stderr, "[cuda]   generate_triangular_surface() -- %s\n", gbt_last_error());
+    } else {
+        const size_t v0 = vertices.size(), t0 = triangles.size();
+        vertices.resize(v0 + (size_t)n * 3);
+        triangles.resize(t0 + (size_t)n);
+        cudaMemcpy(vertices.data() + v0, d_verts, (size_t)n * 9 * sizeof(float), cudaMemcpyDeviceToHost);
+        cudaMemcpy(triangles.data() + t0, d_tris, (size_t)n * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_verts);
+    cudaFree(d_tris);
+}
+
+}  // namespace cuphoto
