@@ -65,6 +65,9 @@ int main(int argc, char** argv) {
             if (depth.empty() || rgb.empty() || !depth.upload(depth_m.data()))
                 throw cuphoto::CuPhotoException("cannot upload the frame");
             cudaMemset2D(rgb.data, rgb.step, 0, (size_t)width * 3, (size_t)height);
+            const std::array<double, 7> pose = tsdf.global_pose();
+            std::printf("pose %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", pose[0], pose[1], pose[2], pose[3],
+                        pose[4], pose[5], pose[6]);
             tsdf.reconstruct_surface(rgb, depth);
         } else {
             const int n = std::atoi(arg(argc, argv, "--frames", "1").c_str());

@@ -102,6 +102,10 @@ def test_headless_example_matches_python_api(gpu, tmp_path, euler):
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     V, F = read_ply(ply)
+    # the pose the C++ layer derived from the configuration (printed in full)
+    used = np.array([float(x) for x in r.stdout.split("pose")[1].split()[:7]])
+    np.testing.assert_allclose(used, pose, rtol=0, atol=1e-12)
+    pose = used
 
     tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=phys, global_offset=off, max_weight=15.0,
                           focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy)
