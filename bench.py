@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=300)
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
+    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene"],
+                    help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames")
     return ap.parse_args()
 
 
@@ -220,10 +222,189 @@ def run_reference_arm(args):
     print(json.dumps(out), flush=True)
 
 
+def multiscene(args, torch, rank, world, local):
+    """16 independent seeded scenes, grids drawn from 64^3..384^3 (multiples of
+    8), 10..120 frames of 640x480 each, all integrated by the batched launches
+    in one captured graph, then a mesh per scene.  With N ranks every rank
+    runs its own 16 scenes (seeds offset by rank)."""
+    import ctypes as C
+    from cuphoto import TSDFVolume, TSDFVolumeConfig, extract_mesh_device
+    from cuphoto import _lib as L
+    from cuphoto import synthetic as S
+    from cuphoto.batch import BatchIntegrator
+    rng = np.random.default_rng(77 + rank)
+    cam = S.Camera()
+    vols, depths, poses, sizes, nfs = [], [], [], [], []
+    for i in range(16):
+        n = int(rng.integers(8, 49)) * 8
+        nf = int(rng.integers(10, 121))
+        sid = 100 * rank + i
+        scene = S.make_scene(scene_id=sid)
+        ps = S.circle_poses(nf, phase=0.1 * i)
+        fr = S.render_sequence_torch(scene, ps, cam, seed=sid)
+        tc = TSDFVolumeConfig(**S.grid_for(n, 2.56), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy,
+                              max_weight=128.0, mode=args.mode)
+        vols.append(TSDFVolume(tc))
+        depths.append([fr[k] for k in range(nf)])
+        poses.append(ps)
+        sizes.append(n)
+        nfs.append(nf)
+    updates = sum(n ** 3 * f for n, f in zip(sizes, nfs))
+    batch = BatchIntegrator(max_scenes=16, max_frames=sum(nfs))
+    # autotune: brick x frames per launch x CTAs/SM on the whole batch
+    if args.config:
+        brick, fpl, ctas = (int(x) for x in args.config.split(","))
+        table = []
+    else:
+        table = []
+        for fpl in (32, 64, 128):
+            for brick in (0, 1, 2, 3):
+                for ctas in (4, 8, 16):
+                    for v in vols:
+                        v.reset()
+                    batch.integrate(vols, depths, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    batch.integrate(vols, depths, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+                    e1.record()
+                    e1.synchronize()
+                    table.append((e0.elapsed_time(e1), brick, fpl, ctas))
+        _, brick, fpl, ctas = min(table)
+    caps = []
+    for v in vols:
+        v.reset()
+    batch.integrate(vols, depths, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+    for v in vols:
+        V, _ = extract_mesh_device(v)
+        caps.append(max(1024, int(len(V) * 1.25) + 1024))
+    outs = [(torch.empty((c, 3, 3), dtype=torch.float32, device="cuda"), torch.empty((c, 3), dtype=torch.int32,
+             device="cuda"), torch.zeros(1, dtype=torch.int64, device="cuda")) for c in caps]
+    lib = L.lib()
+    stream = torch.cuda.Stream()
+
+    def step_integrate():
+        for v in vols:
+            v.reset()
+        batch.integrate(vols, depths, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+
+    def step_mesh():
+        sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for v, (vb, tb, cb), cap in zip(vols, outs, caps):
+            L.check(lib.gbt_extract_mesh_async(v.handle, C.c_void_p(vb.data_ptr()), C.c_void_p(tb.data_ptr()), cap,
+                                               0, C.c_void_p(cb.data_ptr()), sh))
+
+    graphs = []
+    with torch.cuda.stream(stream):
+        step_integrate()
+        step_mesh()
+        torch.cuda.synchronize()
+        for fn in (step_integrate, step_mesh):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                fn()
+            graphs.append(g)
+    g_int, g_mesh = graphs
+    torch.cuda.set_stream(stream)
+    for _ in range(args.warmup):
+        g_int.replay()
+        g_mesh.replay()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            g_int.replay()
+            ev[i][1].record(stream)
+            g_mesh.replay()
+            ev[i][2].record(stream)
+        torch.cuda.synchronize()
+    total_ms = ev[0][0].elapsed_time(ev[-1][2])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    int_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
+    mesh_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
+    ntri = sum(int(o[2].item()) for o in outs)
+    # per scene: the same batched path with one scene
+    per_scene = []
+    for v, ds, ps, n, f in zip(vols, depths, poses, sizes, nfs):
+        v.reset()
+        batch.integrate([v], [ds], [ps], brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.integrate([v], [ds], [ps], brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+        e1.record(stream)
+        e1.synchronize()
+        per_scene.append({"grid": n, "frames": f, "voxel_updates_per_s": n ** 3 * f / (e0.elapsed_time(e1) * 1e-3)})
+    # end to end: depth frames from pinned host memory, integrate, meshes back to the host
+    host = [[torch.empty(d.shape, dtype=d.dtype, pin_memory=True).copy_(d) for d in ds] for ds in depths]
+    torch.cuda.synchronize()
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for hs, ds in zip(host, depths):
+            for h, d in zip(hs, ds):
+                d.copy_(h, non_blocking=True)
+        step_integrate()
+        meshes = [extract_mesh_device(v, capacity=c) for v, c in zip(vols, caps)]
+        d2h = sum(m[0].cpu().numel() * 4 + m[1].cpu().numel() * 4 + 8 for m in meshes)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    h2d = sum(d.numel() * d.element_size() for ds in depths for d in ds)
+    value = world * updates * args.steps / (total_ms * 1e-3)
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: 16 seeded plane + 6 sphere scenes, ray-cast uint16 depth, circle poses",
+        "config": {"workload": "multi-scene batched integrate + marching cubes: 16 volumes %s^3, %s frames 640x480"
+                               % (sizes, nfs),
+                   "mode": args.mode, "frames_per_launch": fpl, "brick": brick, "ctas_per_sm": ctas,
+                   "voxel_updates_per_step": updates, "graph": "resets + batched launches, meshes: CUDA graphs",
+                   "triangles": ntri},
+        "breakdown_ms": {"integrate": int_ms, "mesh": mesh_ms},
+        "integrate_only": {"value": updates / (int_ms * 1e-3), "unit": UNIT},
+        "per_scene": per_scene,
+        "e2e": {"value": world * updates / float(np.mean(e2e)), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e))},
+        "gpu_launches": args.steps * (16 + ((max(nfs) + fpl - 1) // fpl) + 16),
+        "clocks": clocks.summary(),
+        "autotune": {"candidates": len(table)},
+    }
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.workload == "multiscene":
+        import torch
+        rank, world, local = dist_env()
+        torch.cuda.set_device(local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+        eb = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(eb)
+        if rank == 0:
+            eb.build()
+        if world > 1:
+            torch.distributed.barrier()
+        out = multiscene(args, torch, rank, world, local)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return
     import torch
     rank, world, local = dist_env()

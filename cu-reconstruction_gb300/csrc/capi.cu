@@ -1,10 +1,12 @@
 // C ABI of the engine (include/gbt_tsdf.h): volume lifetime, argument
 // checking, pose conversion and kernel dispatch.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -427,6 +429,195 @@ gbt_status gbt_extract_mesh_async(gbt_volume* v, float* verts, int32_t* tris, in
     if (st != GBT_OK) return st;
     cudaError_t e = cudaMemcpyAsync(d_n_tris, a.total, sizeof(long long), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh count copy");
+    return GBT_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched integrate: many volumes, one persistent launch.
+
+struct gbt_batch {
+    int32_t max_scenes;
+    int32_t max_frames;
+    void* host;          // pinned staging: scenes then frames
+    void* dev;           // device tables: ticket (256 B), scenes, frames
+    size_t bytes;
+    cudaEvent_t copied;
+    bool pending;
+};
+
+namespace {
+
+size_t batch_bytes(int32_t max_scenes, int32_t max_frames) {
+    return 256 + (size_t)max_scenes * sizeof(gbt::BatchScene) + (size_t)max_frames * sizeof(gbt::FrameDesc);
+}
+
+}  // namespace
+
+extern "C" {
+
+gbt_status gbt_batch_create(int32_t max_scenes, int32_t max_frames, gbt_batch** out) {
+    if (!out) return fail(GBT_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (max_scenes < 1 || max_frames < 1 || max_scenes > (1 << 20) || max_frames > (1 << 24))
+        return fail(GBT_ERR_INVALID_ARG, "max_scenes %d / max_frames %d out of range", max_scenes, max_frames);
+    gbt_batch* b = new gbt_batch();
+    std::memset(b, 0, sizeof(*b));
+    b->max_scenes = max_scenes;
+    b->max_frames = max_frames;
+    b->bytes = batch_bytes(max_scenes, max_frames);
+    cudaError_t e = cudaMallocHost(&b->host, b->bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dev, b->bytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (b->host) cudaFreeHost(b->host);
+        if (b->dev) cudaFree(b->dev);
+        delete b;
+        return fail(GBT_ERR_ALLOC, "batch tables: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return GBT_OK;
+}
+
+gbt_status gbt_batch_destroy(gbt_batch* b) {
+    if (!b) return GBT_OK;
+    cudaEventSynchronize(b->copied);
+    cudaEventDestroy(b->copied);
+    cudaFreeHost(b->host);
+    cudaFree(b->dev);
+    delete b;
+    return GBT_OK;
+}
+
+gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_t nitems, const gbt_frame* frames,
+                               int32_t nframes, int32_t frames_per_launch, int32_t brick, int32_t ctas_per_sm,
+                               void* stream) {
+    if (!b || !items || !frames) return fail(GBT_ERR_INVALID_ARG, "batch, items or frames is NULL");
+    if (nitems < 1 || nitems > b->max_scenes) return fail(GBT_ERR_INVALID_ARG, "nitems %d outside 1..%d", nitems, b->max_scenes);
+    if (nframes < 1 || nframes > b->max_frames)
+        return fail(GBT_ERR_INVALID_ARG, "nframes %d outside 1..%d", nframes, b->max_frames);
+    if (frames_per_launch < 1 || frames_per_launch > GBT_MAX_FRAMES_PER_SCENE_PASS)
+        return fail(GBT_ERR_INVALID_ARG, "frames_per_launch %d outside 1..%d", frames_per_launch,
+                    GBT_MAX_FRAMES_PER_SCENE_PASS);
+    if (brick < 0 || brick > 3) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..3", brick);
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(GBT_ERR_INVALID_ARG, "ctas_per_sm %d outside 0..32", ctas_per_sm);
+    const gbt_volume* v0 = items[0].volume;
+    if (!v0) return fail(GBT_ERR_INVALID_ARG, "item 0 has no volume");
+    int32_t longest = 0;
+    for (int i = 0; i < nitems; ++i) {
+        const gbt_batch_item& it = items[i];
+        if (!it.volume) return fail(GBT_ERR_INVALID_ARG, "item %d has no volume", i);
+        if (it.volume->cfg.mode != v0->cfg.mode || it.volume->cfg.arith != v0->cfg.arith)
+            return fail(GBT_ERR_INVALID_ARG, "item %d: all volumes of a batch need the same mode and arithmetic", i);
+        if (it.nframes < 0 || it.first_frame < 0 || it.first_frame + it.nframes > nframes)
+            return fail(GBT_ERR_INVALID_ARG, "item %d: frames [%d, %d) outside the frame table", i, it.first_frame,
+                        it.first_frame + it.nframes);
+        for (int j = 0; j < i; ++j) {
+            if (items[j].volume == it.volume) return fail(GBT_ERR_INVALID_ARG, "item %d repeats a volume", i);
+            const bool overlap = it.first_frame < items[j].first_frame + items[j].nframes &&
+                                 items[j].first_frame < it.first_frame + it.nframes;
+            const gbt_volume_cfg& a = it.volume->cfg;
+            const gbt_volume_cfg& c = items[j].volume->cfg;
+            if (overlap && a.mode == GBT_MODE_FIXED &&
+                (a.focal_x != c.focal_x || a.focal_y != c.focal_y || a.cx != c.cx || a.cy != c.cy))
+                return fail(GBT_ERR_INVALID_ARG, "items %d and %d share frames but not intrinsics", j, i);
+        }
+        if (it.nframes > longest) longest = it.nframes;
+    }
+    for (int i = 0; i < nframes; ++i) {
+        gbt_status st = check_frames(frames + i, 1);
+        if (st != GBT_OK) return st;
+    }
+    const int nwin = (longest + frames_per_launch - 1) / frames_per_launch;
+    if (nwin > 64) return fail(GBT_ERR_INVALID_ARG, "%d frames per scene need more than 64 launches", longest);
+    cudaStream_t s = as_stream(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap);
+    // the staging area is rewritten below: wait for the previous call's copy
+    // (a copy recorded into a graph reads the staging area at each replay,
+    // so a graph holds at most one call per batch object)
+    if (b->pending && cap == cudaStreamCaptureStatusNone) cudaEventSynchronize(b->copied);
+    b->pending = false;
+
+    int bx, by, bz;
+    gbt::brick_extent(brick, &bx, &by, &bz);
+    gbt::BatchScene* hs = reinterpret_cast<gbt::BatchScene*>(static_cast<char*>(b->host) + 256);
+    gbt::FrameDesc* hf = reinterpret_cast<gbt::FrameDesc*>(hs + b->max_scenes);
+    for (int i = 0; i < nframes; ++i) {
+        const gbt_frame& f = frames[i];
+        gbt::FrameDesc& fd = hf[i];
+        std::memset(&fd, 0, sizeof(fd));
+        fd.depth = f.depth;
+        fd.pitch = (int64_t)f.pitch_bytes;
+        fd.width = f.width;
+        fd.height = f.height;
+        fd.fmt = f.format;
+        fd.scale = f.depth_scale;
+        fd.q[0] = (float)f.pose[1];
+        fd.q[1] = (float)f.pose[2];
+        fd.q[2] = (float)f.pose[3];
+        fd.q[3] = (float)f.pose[0];
+        fd.t[0] = (float)f.pose[4];
+        fd.t[1] = (float)f.pose[5];
+        fd.t[2] = (float)f.pose[6];
+    }
+    // scenes ordered by frame count, most first: the scenes with frames in a
+    // window are then a prefix of the table
+    std::vector<int> ord(nitems);
+    for (int i = 0; i < nitems; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return items[a].nframes > items[c].nframes; });
+    long long bricks = 0;
+    for (int k = 0; k < nitems; ++k) {
+        const gbt_batch_item& it = items[ord[k]];
+        gbt::BatchScene& sc = hs[k];
+        std::memset(&sc, 0, sizeof(sc));
+        sc.vol = it.volume->desc;
+        sc.first_frame = it.first_frame;
+        sc.nframes = it.nframes;
+        sc.nbx = (sc.vol.nx + bx - 1) / bx;
+        sc.nby = (sc.vol.ny + by - 1) / by;
+        sc.nbz = (sc.vol.nz + bz - 1) / bz;
+        sc.brick_begin = bricks;
+        bricks += (long long)sc.nbx * sc.nby * sc.nbz;
+        if (it.volume->cfg.mode == GBT_MODE_FIXED)
+            for (int f = it.first_frame; f < it.first_frame + it.nframes; ++f)
+                fixed_projection(frames[f].pose, it.volume->cfg, hf[f].P);
+    }
+    if (longest == 0) return GBT_OK;
+
+    const size_t used = 256 + (size_t)b->max_scenes * sizeof(gbt::BatchScene) + (size_t)nframes * sizeof(gbt::FrameDesc);
+    std::memset(b->host, 0, 256);   // one zeroed ticket per launch
+    cudaError_t e = cudaMemcpyAsync(b->dev, b->host, used, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->copied, s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch tables upload");
+    b->pending = cap == cudaStreamCaptureStatusNone;
+
+    char* d = static_cast<char*>(b->dev);
+    const long long per_sm = ctas_per_sm ? ctas_per_sm : gbt::integrate_default_ctas_per_sm();
+    for (int w = 0; w < nwin; ++w) {
+        gbt::BatchArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.ticket = reinterpret_cast<unsigned int*>(d) + w;
+        a.scenes = reinterpret_cast<const gbt::BatchScene*>(d + 256);
+        a.frames = reinterpret_cast<const gbt::FrameDesc*>(a.scenes + b->max_scenes);
+        a.w0 = w * frames_per_launch;
+        a.wn = frames_per_launch;
+        int m = 0;
+        while (m < nitems && hs[m].nframes > a.w0) ++m;
+        a.nscenes = m;
+        a.total_bricks = m < nitems ? hs[m].brick_begin : bricks;
+        long long grid = (long long)device_sms() * per_sm;
+        if (grid > a.total_bricks) grid = a.total_bricks;
+        if (v0->cfg.mode == GBT_MODE_FIXED)
+            e = gbt::launch_batch_fixed(a, brick, (int)grid, s);
+        else if (v0->cfg.arith == GBT_ARITH_IEEE)
+            e = gbt::launch_batch_compat_ieee(a, brick, (int)grid, s);
+        else
+            e = gbt::launch_batch_compat_ref(a, brick, (int)grid, s);
+        if (e != cudaSuccess) return cuda_fail(e, "batch integrate launch");
+    }
     return GBT_OK;
 }
 

@@ -43,6 +43,32 @@ struct IntegrateArgs {
     FrameDesc frames[GBT_MAX_FRAMES_PER_PASS];
 };
 
+// Many volumes in one launch.  A scene's bricks are numbered from
+// brick_begin; frames [first_frame, first_frame + nframes) of the frame table
+// go into its volume.  One launch applies the window [w0, w0 + wn) of every
+// scene's frames (wn <= kBatchMaxFrames); scenes are sorted by frame count,
+// so the scenes with frames in a window are a prefix of the table.
+constexpr int kBatchMaxFrames = GBT_MAX_FRAMES_PER_SCENE_PASS;
+
+struct BatchScene {
+    VolDesc vol;
+    int32_t first_frame;
+    int32_t nframes;
+    int32_t nbx, nby, nbz;
+    int32_t pad0;
+    long long brick_begin;
+};
+
+struct BatchArgs {
+    const BatchScene* scenes;
+    const FrameDesc* frames;
+    int32_t nscenes;        // scenes with frames in this window
+    int32_t w0, wn;         // frame window
+    int32_t pad0;
+    long long total_bricks; // bricks of those scenes
+    unsigned int* ticket;   // this launch's ticket, zero at launch
+};
+
 // Unsigned 32-bit division by a run-time invariant divisor with one
 // multiply-high, after Granlund & Montgomery, "Division by invariant integers
 // using multiplication" (PLDI 1994), figure 4.1.
@@ -101,6 +127,10 @@ cudaError_t launch_integrate_compat_ieee(const IntegrateArgs& a, int brick, int 
 cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
 cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s);
 cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s);
+// Batched integrate (one persistent launch over many volumes).
+cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cudaStream_t s);
+cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s);
+cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 // k_util.cu: volume initialisation and the packed per-voxel transform records.
 cudaError_t launch_volume_init(float* D, float* W, int64_t n, float trunc, cudaStream_t s);
 cudaError_t launch_tvoxels(void* out, const VolDesc& v, cudaStream_t s);

@@ -113,10 +113,8 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, const FastDiv& f) {
 // projected corners when no corner is near the camera plane), with a margin
 // of two pixels and 1e-4 in depth that covers rounding.
 template <int MODE>
-__device__ __forceinline__ bool box_culled(const IntegrateArgs& a, const float* fr, int f, int x_lo, int x_hi,
+__device__ __forceinline__ bool box_culled(const VolDesc& v, const FrameDesc& fd, const float* fr, int x_lo, int x_hi,
                                            int y_lo, int y_hi, int z_lo, int z_hi) {
-    const VolDesc& v = a.vol;
-    const FrameDesc& fd = a.frames[f];
     const float X[2] = {centre(x_lo, v.vs[0], v.off[0]), centre(x_hi, v.vs[0], v.off[0])};
     const float Y[2] = {centre(y_lo, v.vs[1], v.off[1]), centre(y_hi, v.vs[1], v.off[1])};
     const float Zw[2] = {centre(z_lo, v.vs[2], v.off[2]), centre(z_hi, v.vs[2], v.off[2])};
@@ -177,11 +175,202 @@ __device__ __forceinline__ bool box_culled(const IntegrateArgs& a, const float* 
 }
 
 // ---------------------------------------------------------------------------
-// Integrate: one CTA of 128 threads per brick of (4*TX) x BY x BZ voxels; a
-// thread owns 4 consecutive voxels along x, moved as one 16-byte load/store
-// of distance and one of weight.  All frames of the pass are applied to the
-// voxels in registers, in frame order, so a voxel sees exactly the sequence
-// of updates the per-frame reference loop would apply.
+// Integrate.  One CTA of 128 threads works on a brick of (4*TX) x BY x BZ
+// voxels; a thread owns 4 consecutive voxels along x, moved as one 16-byte
+// load/store of distance and one of weight.  All frames of the pass are
+// applied to the voxels in registers, in frame order, so a voxel sees exactly
+// the sequence of updates the per-frame reference loop would apply.
+
+// Per-frame pose table entry: compat -> rotation (9) + translation (3),
+// fixed -> the three rows of K[R|t].
+template <int MODE>
+__device__ __forceinline__ void load_pose(const FrameDesc& fd, float* dst) {
+    if (MODE == kCompat) {
+        float R[9];
+        compat_rotation(fd.q, R);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) dst[k] = R[k];
+        dst[9] = fd.t[0];
+        dst[10] = fd.t[1];
+        dst[11] = fd.t[2];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) dst[k] = fd.P[k];
+    }
+}
+
+// The thread's place in a brick and its warp's sub-box.
+template <int TX, int BY, int BZ>
+struct BrickLayout {
+    int tx, ty, tz, lane, wy_lo, wy_hi, wz_lo, wz_hi;
+    __device__ __forceinline__ BrickLayout(int tid) {
+        tx = tid % TX;
+        ty = (tid / TX) % BY;
+        tz = tid / (TX * BY);
+        lane = tid & 31;
+        const int wfirst = tid & ~31;
+        wy_lo = (TX * BY >= 32) ? (wfirst / TX) % BY : 0;
+        wy_hi = (TX * BY >= 32) ? wy_lo + 32 / TX - 1 : BY - 1;
+        wz_lo = wfirst / (TX * BY);
+        wz_hi = (wfirst + 31) / (TX * BY);
+    }
+};
+
+// Lane f of the warp tests frame f0 + f against the warp's sub-box; returns
+// the mask of frames that may update a voxel of it.
+template <int MODE, int TX, int BY, int BZ>
+__device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const FrameDesc* frames, const float (*pose)[12],
+                                                     int f0, int nf, const BrickLayout<TX, BY, BZ>& L, int bx0,
+                                                     int by0, int bz0) {
+    bool live = false;
+    const int f = f0 + L.lane;
+    if (f < nf) {
+        const int xl = bx0, xh = min(bx0 + 4 * TX, v.nx) - 1;
+        const int yl = by0 + L.wy_lo, yh = min(by0 + L.wy_hi, v.ny - 1);
+        const int zl = bz0 + L.wz_lo, zh = min(bz0 + L.wz_hi, v.nz - 1);
+        live = (yl <= yh && zl <= zh) && !box_culled<MODE>(v, frames[f], pose[f], xl, xh, yl, yh, zl, zh);
+    }
+    return __ballot_sync(0xffffffffu, live);
+}
+
+// Applies one frame to the thread's (up to) 4 voxels; returns whether any changed.
+template <int MODE>
+__device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& fd, const float* pr, const float* px,
+                                            float py, float pz, int nvalid, float* d, float* w, const float* s_inv) {
+    bool dirty = false;
+    const char* dimg = static_cast<const char*>(fd.depth);
+    const int64_t pitch = fd.pitch;
+    const uint32_t width = (uint32_t)fd.width, height = (uint32_t)fd.height;
+    if (MODE == kCompat) {
+        const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
+        const float r6 = pr[6], r7 = pr[7], r8 = pr[8], t0 = pr[9], t1 = pr[10], t2 = pr[11];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i >= nvalid) break;
+            // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51)
+            int u = 0, vv = 0;
+            if (pz != 0.f) {
+                const float cxv = compat_cam(r0, r1, r2, t0, px[i], py, pz);
+                const float cyv = compat_cam(r3, r4, r5, t1, px[i], py, pz);
+                const float czv = compat_cam(r6, r7, r8, t2, px[i], py, pz);
+                if (czv != 0.f) {
+                    u = (int)compat_q(cxv, v.fx, czv, v.cx);
+                    vv = (int)compat_q(cyv, v.fy, czv, v.cy);
+                }
+            }
+            // tsdf_volume.cu:166-187
+            if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
+            const char* row = dimg + (int64_t)vv * pitch;
+            // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
+            // (rgbd_dataset.cpp:29): one float multiply
+            const float dv = fd.fmt == GBT_DEPTH_U16
+                                 ? u16_metres(__ldg(reinterpret_cast<const unsigned short*>(row) + u), fd.scale)
+                                 : __ldg(reinterpret_cast<const float*>(row) + u);
+            if (dv <= 0.0f || dv > 24.0) continue;
+            const float sdf = dv - pz;
+            if (sdf >= -v.trunc) {
+                float tsdf = sdf;
+                if (sdf > 0) tsdf = fminf(sdf, v.trunc);
+                const float nw = w[i] + 1.0f;
+                const float nd = compat_avg(d[i], w[i], tsdf, nw);
+                w[i] = nw;
+                d[i] = nd;
+                dirty = true;
+            }
+        }
+    } else {
+#if !defined(GBT_REF_ARITH)
+        const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
+        const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
+        const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
+        const int fmt = fd.fmt;
+        const float scale = fd.scale;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i >= nvalid) break;
+            const float Z = __fmaf_rn(pr[8], px[i], aZ);
+            if (!(Z > v.min_z)) continue;
+            const float U = __fmaf_rn(pr[0], px[i], aU);
+            const float V = __fmaf_rn(pr[4], px[i], aV);
+            const float rz = __frcp_rn(Z);
+            const int u = __float2int_rn(__fmul_rn(U, rz));
+            const int vv = __float2int_rn(__fmul_rn(V, rz));
+            if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
+            const char* row = dimg + (int64_t)vv * pitch;
+            float dv;
+            if (fmt == GBT_DEPTH_U16)
+                dv = __fmul_rn((float)__ldg(reinterpret_cast<const unsigned short*>(row) + u), scale);
+            else
+                dv = __ldg(reinterpret_cast<const float*>(row) + u);
+            if (!(dv > 0.f && dv <= v.max_depth)) continue;
+            const float sdf = __fsub_rn(dv, Z);
+            if (!(sdf >= -v.trunc)) continue;
+            const float tsdf = fminf(sdf, v.trunc);
+            const int n = max(__float2int_rz(w[i]), 0) + 1;
+            const float inv = n < 256 ? s_inv[n] : __frcp_rn((float)n);
+            d[i] = __fmaf_rn(__fsub_rn(tsdf, d[i]), inv, d[i]);
+            w[i] = fminf(__fadd_rn(w[i], 1.0f), v.max_weight);
+            dirty = true;
+        }
+#endif
+    }
+    return dirty;
+}
+
+// The thread's voxels of a brick: load, centres, store.
+struct ThreadVoxels {
+    size_t base;
+    int x0, y, z, nvalid;
+    bool full;
+    float d[4], w[4], px[4], py, pz;
+
+    __device__ __forceinline__ bool init(const VolDesc& v, int x0_, int y_, int z_) {
+        x0 = x0_;
+        y = y_;
+        z = z_;
+        if (y >= v.ny || z >= v.nz || x0 >= v.nx) return false;
+        base = ((size_t)z * v.ny + y) * v.nx + x0;
+        full = ((v.nx & 3) == 0) && (x0 + 3 < v.nx);
+        nvalid = min(4, v.nx - x0);
+        return true;
+    }
+    __device__ __forceinline__ void load(const VolDesc& v) {
+        if (full) {
+            const float4 d4 = *reinterpret_cast<const float4*>(v.D + base);
+            const float4 w4 = *reinterpret_cast<const float4*>(v.W + base);
+            d[0] = d4.x; d[1] = d4.y; d[2] = d4.z; d[3] = d4.w;
+            w[0] = w4.x; w[1] = w4.y; w[2] = w4.z; w[3] = w4.w;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                d[i] = (i < nvalid) ? v.D[base + i] : 0.f;
+                w[i] = (i < nvalid) ? v.W[base + i] : 0.f;
+            }
+        }
+        py = centre(y, v.vs[1], v.off[1]);
+        pz = centre(z, v.vs[2], v.off[2]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) px[i] = centre(x0 + i, v.vs[0], v.off[0]);
+    }
+    __device__ __forceinline__ void store(const VolDesc& v) const {
+        if (full) {
+            *reinterpret_cast<float4*>(v.D + base) = make_float4(d[0], d[1], d[2], d[3]);
+            *reinterpret_cast<float4*>(v.W + base) = make_float4(w[0], w[1], w[2], w[3]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i < nvalid) {
+                    v.D[base + i] = d[i];
+                    v.W[base + i] = w[i];
+                }
+        }
+    }
+};
+
+__device__ __forceinline__ void fill_inv_table(float* s_inv) {
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) s_inv[k] = k ? __frcp_rn((float)k) : 0.f;
+}
+
 template <int MODE, int TX, int BY, int BZ>
 __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ IntegrateArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
@@ -192,180 +381,100 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
     const VolDesc& v = a.vol;
     const int tid = threadIdx.x;
     const int nf = a.nframes;
-    if (tid < nf) {
-        const FrameDesc& fd = a.frames[tid];
-        if (MODE == kCompat) {
-            float R[9];
-            compat_rotation(fd.q, R);
-#pragma unroll
-            for (int k = 0; k < 9; ++k) s_pose[tid][k] = R[k];
-            s_pose[tid][9] = fd.t[0];
-            s_pose[tid][10] = fd.t[1];
-            s_pose[tid][11] = fd.t[2];
-        } else {
-#pragma unroll
-            for (int k = 0; k < 12; ++k) s_pose[tid][k] = fd.P[k];
-        }
-    }
-    if (MODE == kFixed) {
-        for (int k = tid; k < 256; k += 128) s_inv[k] = k ? __frcp_rn((float)k) : 0.f;
-    }
+    if (tid < nf) load_pose<MODE>(a.frames[tid], s_pose[tid]);
+    if (MODE == kFixed) fill_inv_table(s_inv);
     __syncthreads();
 
-    const int tx = tid % TX, ty = (tid / TX) % BY, tz = tid / (TX * BY);
-    const int lane = tid & 31;
-    const int wfirst = tid & ~31;
-    // the warp's sub-box inside the brick
-    const int wy_lo = (TX * BY >= 32) ? (wfirst / TX) % BY : 0;
-    const int wy_hi = (TX * BY >= 32) ? wy_lo + 32 / TX - 1 : BY - 1;
-    const int wz_lo = wfirst / (TX * BY);
-    const int wz_hi = (wfirst + 31) / (TX * BY);
-
-    const int nx = v.nx, ny = v.ny, nz = v.nz;
+    const BrickLayout<TX, BY, BZ> L(tid);
     const int BXV = 4 * TX;
-    const int nbx = (nx + BXV - 1) / BXV, nby = (ny + BY - 1) / BY, nbz = (nz + BZ - 1) / BZ;
+    const int nbx = (v.nx + BXV - 1) / BXV, nby = (v.ny + BY - 1) / BY, nbz = (v.nz + BZ - 1) / BZ;
     const long long nbricks = (long long)nbx * nby * nbz;
-    const bool vec_ok = (nx & 3) == 0;
-    const uint32_t all_frames = nf >= 32 ? 0xffffffffu : ((1u << nf) - 1u);
 
     for (long long b = blockIdx.x; b < nbricks; b += gridDim.x) {
         const int bxi = (int)(b % nbx);
         const long long rest = b / nbx;
-        const int byi = (int)(rest % nby);
-        const int bzi = (int)(rest / nby);
-        const int bx0 = bxi * BXV, by0 = byi * BY, bz0 = bzi * BZ;
-
+        const int bx0 = bxi * BXV, by0 = (int)(rest % nby) * BY, bz0 = (int)(rest / nby) * BZ;
         // frames for which this warp's box may contain an updated voxel
-        bool live = false;
-        if (lane < nf) {
-            const int xl = bx0, xh = min(bx0 + BXV, nx) - 1;
-            const int yl = by0 + wy_lo, yh = min(by0 + wy_hi, ny - 1);
-            const int zl = bz0 + wz_lo, zh = min(bz0 + wz_hi, nz - 1);
-            live = (yl <= yh && zl <= zh) && !box_culled<MODE>(a, s_pose[lane], lane, xl, xh, yl, yh, zl, zh);
-        }
-        const uint32_t fmask = __ballot_sync(0xffffffffu, live) & all_frames;
+        const uint32_t fmask = warp_live_frames<MODE>(v, a.frames, s_pose, 0, nf, L, bx0, by0, bz0);
         if (fmask == 0u) continue;
-
-        const int x0 = bx0 + 4 * tx, y = by0 + ty, z = bz0 + tz;
-        if (y >= ny || z >= nz || x0 >= nx) continue;
-        const size_t base = ((size_t)z * ny + y) * nx + x0;
-        const bool full = vec_ok && (x0 + 3 < nx);
-        float d[4], w[4];
-        if (full) {
-            const float4 d4 = *reinterpret_cast<const float4*>(v.D + base);
-            const float4 w4 = *reinterpret_cast<const float4*>(v.W + base);
-            d[0] = d4.x; d[1] = d4.y; d[2] = d4.z; d[3] = d4.w;
-            w[0] = w4.x; w[1] = w4.y; w[2] = w4.z; w[3] = w4.w;
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                d[i] = (x0 + i < nx) ? v.D[base + i] : 0.f;
-                w[i] = (x0 + i < nx) ? v.W[base + i] : 0.f;
-            }
-        }
-        const float py = centre(y, v.vs[1], v.off[1]);
-        const float pz = centre(z, v.vs[2], v.off[2]);
-        float px[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) px[i] = centre(x0 + i, v.vs[0], v.off[0]);
-        const int nvalid = min(4, nx - x0);
+        ThreadVoxels t;
+        if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
+        t.load(v);
         bool dirty = false;
-
-        uint32_t m = fmask;
-        while (m) {
+        for (uint32_t m = fmask; m; m &= m - 1) {
             const int f = __ffs(m) - 1;
-            m &= m - 1;
-            const FrameDesc& fd = a.frames[f];
-            const char* dimg = static_cast<const char*>(fd.depth);
-            const int64_t pitch = fd.pitch;
-            const uint32_t width = (uint32_t)fd.width, height = (uint32_t)fd.height;
-            const float* pr = s_pose[f];
-            if (MODE == kCompat) {
-                const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
-                const float r6 = pr[6], r7 = pr[7], r8 = pr[8], t0 = pr[9], t1 = pr[10], t2 = pr[11];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    if (i >= nvalid) break;
-                    // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51)
-                    int u = 0, vv = 0;
-                    if (pz != 0.f) {
-                        const float cxv = compat_cam(r0, r1, r2, t0, px[i], py, pz);
-                        const float cyv = compat_cam(r3, r4, r5, t1, px[i], py, pz);
-                        const float czv = compat_cam(r6, r7, r8, t2, px[i], py, pz);
-                        if (czv != 0.f) {
-                            u = (int)compat_q(cxv, v.fx, czv, v.cx);
-                            vv = (int)compat_q(cyv, v.fy, czv, v.cy);
-                        }
-                    }
-                    // tsdf_volume.cu:166-187
-                    if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
-                    const char* row = dimg + (int64_t)vv * pitch;
-                    // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
-                    // (rgbd_dataset.cpp:29): one float multiply
-                    const float dv = fd.fmt == GBT_DEPTH_U16
-                                         ? u16_metres(__ldg(reinterpret_cast<const unsigned short*>(row) + u), fd.scale)
-                                         : __ldg(reinterpret_cast<const float*>(row) + u);
-                    if (dv <= 0.0f || dv > 24.0) continue;
-                    const float sdf = dv - pz;
-                    if (sdf >= -v.trunc) {
-                        float tsdf = sdf;
-                        if (sdf > 0) tsdf = fminf(sdf, v.trunc);
-                        const float nw = w[i] + 1.0f;
-                        const float nd = compat_avg(d[i], w[i], tsdf, nw);
-                        w[i] = nw;
-                        d[i] = nd;
-                        dirty = true;
-                    }
-                }
-            } else {
-#if !defined(GBT_REF_ARITH)
-                const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
-                const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
-                const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
-                const int fmt = fd.fmt;
-                const float scale = fd.scale;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    if (i >= nvalid) break;
-                    const float Z = __fmaf_rn(pr[8], px[i], aZ);
-                    if (!(Z > v.min_z)) continue;
-                    const float U = __fmaf_rn(pr[0], px[i], aU);
-                    const float V = __fmaf_rn(pr[4], px[i], aV);
-                    const float rz = __frcp_rn(Z);
-                    const int u = __float2int_rn(__fmul_rn(U, rz));
-                    const int vv = __float2int_rn(__fmul_rn(V, rz));
-                    if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
-                    const char* row = dimg + (int64_t)vv * pitch;
-                    float dv;
-                    if (fmt == GBT_DEPTH_U16)
-                        dv = __fmul_rn((float)__ldg(reinterpret_cast<const unsigned short*>(row) + u), scale);
-                    else
-                        dv = __ldg(reinterpret_cast<const float*>(row) + u);
-                    if (!(dv > 0.f && dv <= v.max_depth)) continue;
-                    const float sdf = __fsub_rn(dv, Z);
-                    if (!(sdf >= -v.trunc)) continue;
-                    const float tsdf = fminf(sdf, v.trunc);
-                    const int n = max(__float2int_rz(w[i]), 0) + 1;
-                    const float inv = n < 256 ? s_inv[n] : __frcp_rn((float)n);
-                    d[i] = __fmaf_rn(__fsub_rn(tsdf, d[i]), inv, d[i]);
-                    w[i] = fminf(__fadd_rn(w[i], 1.0f), v.max_weight);
-                    dirty = true;
-                }
-#endif
+            dirty |= apply_frame<MODE>(v, a.frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, t.d, t.w, s_inv);
+        }
+        if (dirty) t.store(v);
+    }
+}
+
+// Many volumes (scenes) in one persistent launch.  Work items are bricks,
+// numbered scene after scene in the order of the scene table (the host sorts
+// scenes by frames per voxel, most expensive first); CTAs take the next brick
+// from an atomic ticket, so uneven scenes balance dynamically.  A brick of a
+// scene receives all of that scene's frames, in order, in registers.
+template <int MODE, int TX, int BY, int BZ>
+__global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_constant__ BatchArgs a) {
+    static_assert(TX * BY * BZ == 128, "128 threads per CTA");
+    __shared__ float s_pose[kBatchMaxFrames][12];
+    __shared__ float s_inv[256];
+    __shared__ long long s_task;
+    __shared__ int s_scene;
+
+    const int tid = threadIdx.x;
+    if (MODE == kFixed) fill_inv_table(s_inv);
+    const BrickLayout<TX, BY, BZ> L(tid);
+    const int BXV = 4 * TX;
+    int scene = -1;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const long long task = (long long)atomicAdd(a.ticket, 1u);
+            int sc = scene < 0 ? 0 : scene;
+            if (task < a.total_bricks) {
+                while (sc + 1 < a.nscenes && a.scenes[sc + 1].brick_begin <= task) ++sc;
+                while (sc > 0 && a.scenes[sc].brick_begin > task) --sc;
             }
+            s_task = task;
+            s_scene = sc;
         }
-        if (!dirty) continue;
-        if (full) {
-            *reinterpret_cast<float4*>(v.D + base) = make_float4(d[0], d[1], d[2], d[3]);
-            *reinterpret_cast<float4*>(v.W + base) = make_float4(w[0], w[1], w[2], w[3]);
-        } else {
+        __syncthreads();
+        const long long task = s_task;
+        if (task >= a.total_bricks) return;
+        const BatchScene& S = a.scenes[s_scene];
+        const VolDesc& v = S.vol;
+        const FrameDesc* frames = a.frames + S.first_frame + a.w0;
+        const int nf = min(S.nframes - a.w0, a.wn);
+        if (s_scene != scene) {
+            scene = s_scene;
+            for (int f = tid; f < nf; f += blockDim.x) load_pose<MODE>(frames[f], s_pose[f]);
+            __syncthreads();
+        }
+        const long long b = task - S.brick_begin;
+        const int bxi = (int)(b % S.nbx);
+        const long long rest = b / S.nbx;
+        const int bx0 = bxi * BXV, by0 = (int)(rest % S.nby) * BY, bz0 = (int)(rest / S.nby) * BZ;
+
+        uint32_t masks[kBatchMaxFrames / 32];
+        bool any = false;
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (x0 + i < nx) {
-                    v.D[base + i] = d[i];
-                    v.W[base + i] = w[i];
-                }
+        for (int c = 0; c < kBatchMaxFrames / 32; ++c) {
+            masks[c] = (c * 32 < nf) ? warp_live_frames<MODE>(v, frames, s_pose, c * 32, nf, L, bx0, by0, bz0) : 0u;
+            any |= masks[c] != 0u;
         }
+        if (!any) continue;
+        ThreadVoxels t;
+        if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
+        t.load(v);
+        bool dirty = false;
+#pragma unroll
+        for (int c = 0; c < kBatchMaxFrames / 32; ++c)
+            for (uint32_t m = masks[c]; m; m &= m - 1) {
+                const int f = c * 32 + __ffs(m) - 1;
+                dirty |= apply_frame<MODE>(v, frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, t.d, t.w, s_inv);
+            }
+        if (dirty) t.store(v);
     }
 }
 
@@ -596,6 +705,22 @@ cudaError_t launch_integrate_mode(const IntegrateArgs& a, int brick, int grid, c
         case 2: return launch_integrate_shape<MODE, 8, 2, 8>(a, grid, s);
         case 3: return launch_integrate_shape<MODE, 16, 2, 4>(a, grid, s);
         default: return launch_integrate_shape<MODE, 8, 4, 4>(a, grid, s);
+    }
+}
+
+template <int MODE, int TX, int BY, int BZ>
+cudaError_t launch_batch_shape(const BatchArgs& a, int grid, cudaStream_t s) {
+    integrate_batch_kernel<MODE, TX, BY, BZ><<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_batch_mode(const BatchArgs& a, int brick, int grid, cudaStream_t s) {
+    switch (brick) {
+        case 1: return launch_batch_shape<MODE, 4, 8, 4>(a, grid, s);
+        case 2: return launch_batch_shape<MODE, 8, 2, 8>(a, grid, s);
+        case 3: return launch_batch_shape<MODE, 16, 2, 4>(a, grid, s);
+        default: return launch_batch_shape<MODE, 8, 4, 4>(a, grid, s);
     }
 }
 

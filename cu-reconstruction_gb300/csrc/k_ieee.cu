@@ -16,6 +16,14 @@ cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, 
     return launch_integrate_mode<kFixed>(a, brick, grid, s);
 }
 
+cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s) {
+    return launch_batch_mode<kCompat>(a, brick, grid, s);
+}
+
+cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStream_t s) {
+    return launch_batch_mode<kFixed>(a, brick, grid, s);
+}
+
 cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kCompat>(a, s); }
 
 cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kFixed>(a, s); }

@@ -73,6 +73,12 @@ class Frame(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("first_frame", C.c_int32), ("nframes", C.c_int32)]
+
+
+MAX_FRAMES_PER_SCENE_PASS = 128
+
 # (name, restype, argtypes) of every exported entry point, in header order.
 SIGNATURES = [
     ("gbt_volume_create", C.c_int, [C.POINTER(VolumeCfg), C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -82,6 +88,10 @@ SIGNATURES = [
     ("gbt_volume_transformation_voxels", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_integrate", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_void_p]),
     ("gbt_integrate_tuned", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    ("gbt_batch_create", C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("gbt_batch_destroy", C.c_int, [C.c_void_p]),
+    ("gbt_integrate_batch", C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int32, C.POINTER(Frame), C.c_int32,
+                                      C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     ("gbt_extract_mesh", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                    C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,

@@ -148,6 +148,36 @@ gbt_status gbt_integrate(gbt_volume* vol, const gbt_frame* frames, int32_t nfram
 gbt_status gbt_integrate_tuned(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, int32_t brick,
                                int32_t ctas_per_sm, void* stream);
 
+/* Batched integrate: many volumes ("scenes") of any grid sizes, each with its
+ * own frames, in persistent launches that cover all scenes at once.  Extends
+ * TSDFVolume::integrate (tsdf_volume.cu:257-290) to many volumes; the
+ * reference has no batched form.
+ *
+ * Item i applies frames[first_frame .. first_frame + nframes) to its volume,
+ * in order.  One launch applies the next frames_per_launch (1..128) frames of
+ * every scene, so a call makes ceil(longest sequence / frames_per_launch)
+ * launches (at most 64).  Volumes of one call must share mode and arithmetic
+ * and be distinct; items may share frames only when their intrinsics agree.
+ * Results are bit-identical to gbt_integrate on each volume.
+ *
+ * A gbt_batch owns the device tables of a call (scene and frame descriptors,
+ * launch tickets) and a pinned staging copy: a call allocates nothing and
+ * records into a CUDA graph as one copy and its launches.  A replay re-reads
+ * the staging area as the last call on the batch object left it, so a graph
+ * should hold one call per batch object.  One host thread per batch object. */
+#define GBT_MAX_FRAMES_PER_SCENE_PASS 128
+typedef struct gbt_batch gbt_batch;
+typedef struct {
+    gbt_volume* volume;
+    int32_t first_frame;
+    int32_t nframes;
+} gbt_batch_item;
+gbt_status gbt_batch_create(int32_t max_scenes, int32_t max_frames, gbt_batch** out);
+gbt_status gbt_batch_destroy(gbt_batch* batch);
+gbt_status gbt_integrate_batch(gbt_batch* batch, const gbt_batch_item* items, int32_t nitems, const gbt_frame* frames,
+                               int32_t nframes, int32_t frames_per_launch, int32_t brick, int32_t ctas_per_sm,
+                               void* stream);
+
 /* Replaces generate_triangular_surface (marching_cubes.cu:191-237).
  * Writes up to cap_tris triangles: verts gets 9 floats per triangle (three
  * vertices, no sharing, as the reference emits them) and tris gets 3 ints per

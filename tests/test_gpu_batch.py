@@ -1,0 +1,90 @@
+"""Batched integrate (many volumes, one persistent launch) against the
+single-volume path, through the C ABI."""
+import numpy as np
+import pytest
+
+from cuphoto import TSDFVolume, TSDFVolumeConfig
+from cuphoto import synthetic as S
+from cuphoto.batch import BatchIntegrator
+
+from helpers import dev_depth
+
+pytestmark = pytest.mark.gpu
+
+SCENES = [((64, 64, 64), 10), ((40, 56, 72), 37), ((96, 80, 48), 140), ((20, 20, 20), 1), ((33, 17, 9), 5)]
+
+
+def scene_data(gpu, mode, arith="reference"):
+    cam = S.Camera.half()
+    vols, depths, poses, cfgs = [], [], [], []
+    for i, (grid, nf) in enumerate(SCENES):
+        seq = S.make_sequence(nf, scene_id=10 + i, camera=cam, trajectory="circle")
+        tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=tuple(2.56 * g / max(grid) for g in grid),
+                              global_offset=(-1.28, -1.0, -1.28), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx,
+                              cy=cam.cy, mode=mode, arith=arith, max_weight=20)
+        cfgs.append(tc)
+        vols.append(TSDFVolume(tc))
+        d = seq.depth_u16 if mode == "fixed" or i % 2 else seq.depth_m()
+        depths.append([dev_depth(gpu, x) for x in d])
+        poses.append(seq.poses)
+    return cfgs, vols, depths, poses
+
+
+@pytest.mark.parametrize("mode,arith", [("fixed", "ieee"), ("compat", "reference"), ("compat", "ieee")])
+@pytest.mark.parametrize("brick", [0, 1])
+def test_batch_equals_per_volume_integrate(gpu, mode, arith, brick):
+    cfgs, vols, depths, poses = scene_data(gpu, mode, arith)
+    BatchIntegrator(max_scenes=8, max_frames=512).integrate(vols, depths, poses, brick=brick, ctas_per_sm=4)
+    gpu.cuda.synchronize()
+    for tc, vol, ds, ps in zip(cfgs, vols, depths, poses):
+        ref = TSDFVolume(tc)
+        ref.integrate_sequence(ds, ps, frames_per_pass=32)
+        gpu.cuda.synchronize()
+        W0, W1 = ref.voxel_weights_data().cpu().numpy(), vol.voxel_weights_data().cpu().numpy()
+        D0, D1 = ref.voxel_distances_data().cpu().numpy(), vol.voxel_distances_data().cpu().numpy()
+        assert np.array_equal(W0, W1)
+        assert np.array_equal(D0.view(np.uint32), D1.view(np.uint32))
+    assert (vols[2].voxel_weights_data() > 0).float().mean().item() > 0.05
+
+
+def test_batch_chunks_and_graph_replay(gpu):
+    """Frames split over launches of 16 per scene, recorded in a CUDA graph and
+    replayed: the same volumes as one direct call."""
+    cfgs, vols, depths, poses = scene_data(gpu, "fixed", "ieee")
+    b = BatchIntegrator(max_scenes=8, max_frames=512)
+    stream = gpu.cuda.Stream()
+    with gpu.cuda.stream(stream):
+        for v in vols:
+            v.reset()
+        b.integrate(vols, depths, poses, frames_per_launch=16)
+        gpu.cuda.synchronize()
+        g = gpu.cuda.CUDAGraph()
+        with gpu.cuda.graph(g, stream=stream):
+            for v in vols:
+                v.reset()
+            b.integrate(vols, depths, poses, frames_per_launch=16)
+    gpu.cuda.synchronize()
+    for v in vols:
+        v.voxel_weights_data().fill_(-7.0)
+    gpu.cuda.synchronize()
+    with gpu.cuda.stream(stream):
+        g.replay()
+    gpu.cuda.synchronize()
+    for tc, vol, ds, ps in zip(cfgs, vols, depths, poses):
+        ref = TSDFVolume(tc)
+        ref.integrate_sequence(ds, ps, frames_per_pass=32)
+        gpu.cuda.synchronize()
+        assert np.array_equal(ref.voxel_weights_data().cpu().numpy(), vol.voxel_weights_data().cpu().numpy())
+        assert np.array_equal(ref.voxel_distances_data().cpu().numpy().view(np.uint32),
+                              vol.voxel_distances_data().cpu().numpy().view(np.uint32))
+
+
+def test_batch_rejects_mixed_modes(gpu):
+    from cuphoto import _lib as L
+    import ctypes as C
+    a = TSDFVolume(TSDFVolumeConfig(voxel_grid_size=(8, 8, 8), physical_size=(1, 1, 1)))
+    b = TSDFVolume(TSDFVolumeConfig(voxel_grid_size=(8, 8, 8), physical_size=(1, 1, 1), mode="fixed"))
+    d = gpu.zeros((4, 4), dtype=gpu.float32, device="cuda")
+    bi = BatchIntegrator(4, 8)
+    with pytest.raises(L.GbtError, match="same mode"):
+        bi.integrate([a, b], [[d], [d]], [[np.array([1.0, 0, 0, 0, 0, 0, 0])]] * 2)
