@@ -232,6 +232,7 @@ gbt_status gbt_volume_destroy(gbt_volume* v) {
 
 gbt_status gbt_volume_reset(gbt_volume* v, void* stream) {
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    cudaGetLastError();  // a launch reports only its own failure
     cudaError_t e = gbt::launch_volume_init(v->desc.D, v->desc.W, v->nvox, v->desc.trunc, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "volume initialisation");
     return GBT_OK;
@@ -265,6 +266,7 @@ gbt_status gbt_volume_transformation_voxels(gbt_volume* v, void* stream, void** 
             v->tvox = nullptr;
             return fail(GBT_ERR_ALLOC, "allocating %zu bytes of voxel transforms: %s", bytes, cudaGetErrorString(e));
         }
+        cudaGetLastError();
         e = gbt::launch_tvoxels(v->tvox, v->desc, as_stream(stream));
         if (e != cudaSuccess) return cuda_fail(e, "voxel transforms");
     }
@@ -310,6 +312,7 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     if (grid > nbricks) grid = nbricks;
     if (grid < 1) grid = 1;
     cudaError_t e;
+    cudaGetLastError();  // a launch reports only its own failure
     if (v->cfg.mode == GBT_MODE_FIXED)
         e = gbt::launch_integrate_fixed(a, brick, (int)grid, as_stream(stream));
     else if (v->cfg.arith == GBT_ARITH_IEEE)
@@ -376,6 +379,7 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
 }
 
 gbt_status mc_launch(gbt_volume* v, const gbt::McArgs& a, cudaStream_t s) {
+    cudaGetLastError();  // a launch reports only its own failure
     cudaError_t e = cudaMemsetAsync(v->mc_scratch, 0, 64 + (size_t)a.ntiles * 8, s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh scratch clear");
     if (a.ntiles == 0) return GBT_OK;
@@ -483,7 +487,7 @@ gbt_status gbt_batch_create(int32_t max_scenes, int32_t max_frames, gbt_batch** 
 
 gbt_status gbt_batch_destroy(gbt_batch* b) {
     if (!b) return GBT_OK;
-    cudaEventSynchronize(b->copied);
+    if (b->pending) cudaEventSynchronize(b->copied);
     cudaEventDestroy(b->copied);
     cudaFreeHost(b->host);
     cudaFree(b->dev);
@@ -595,6 +599,7 @@ gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_
     b->pending = cap == cudaStreamCaptureStatusNone;
 
     char* d = static_cast<char*>(b->dev);
+    cudaGetLastError();  // a launch reports only its own failure
     const long long per_sm = ctas_per_sm ? ctas_per_sm : gbt::integrate_default_ctas_per_sm();
     for (int w = 0; w < nwin; ++w) {
         gbt::BatchArgs a;
