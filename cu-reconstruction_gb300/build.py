@@ -26,6 +26,7 @@ UNITS = {
     "k_util.cu": [],
     "capi.cu": [],
     "k_noalloc.cu": [],
+    "k_diff.cu": [],
 }
 
 

@@ -627,3 +627,92 @@ gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiable integrate.
+
+namespace {
+
+gbt_status diff_args(const gbt_diff_cfg* c, int32_t nframes, gbt::DiffArgs* a) {
+    if (!c) return fail(GBT_ERR_INVALID_ARG, "cfg is NULL");
+    if (c->dtype != 0 && c->dtype != 1) return fail(GBT_ERR_INVALID_ARG, "dtype %d is not 0 or 1", c->dtype);
+    for (int i = 0; i < 3; ++i)
+        if (c->voxel_grid_size[i] == 0 || !(c->voxel_size[i] > 0.f))
+            return fail(GBT_ERR_INVALID_ARG, "grid/voxel size %d must be positive", i);
+    const int64_t n = (int64_t)c->voxel_grid_size[0] * c->voxel_grid_size[1] * c->voxel_grid_size[2];
+    if (n >= (int64_t)1 << 32) return fail(GBT_ERR_INVALID_ARG, "more than 2^32-1 voxels");
+    if (!(c->truncation > 0.f) || !(c->max_weight >= 1.f) || !(c->max_depth > 0.f))
+        return fail(GBT_ERR_INVALID_ARG, "truncation, max_depth must be > 0 and max_weight >= 1");
+    if (c->width < 2 || c->height < 2) return fail(GBT_ERR_INVALID_ARG, "depth images need at least 2x2 pixels");
+    if (nframes < 1 || nframes > GBT_MAX_FRAMES_PER_SCENE_PASS)
+        return fail(GBT_ERR_INVALID_ARG, "nframes %d outside 1..%d", nframes, GBT_MAX_FRAMES_PER_SCENE_PASS);
+    std::memset(a, 0, sizeof(*a));
+    a->nx = (int32_t)c->voxel_grid_size[0];
+    a->ny = (int32_t)c->voxel_grid_size[1];
+    a->nz = (int32_t)c->voxel_grid_size[2];
+    for (int i = 0; i < 3; ++i) {
+        a->vs[i] = c->voxel_size[i];
+        a->off[i] = c->global_offset[i];
+    }
+    a->fx = c->focal_x;
+    a->fy = c->focal_y;
+    a->cx = c->cx;
+    a->cy = c->cy;
+    a->trunc = c->truncation;
+    a->max_weight = c->max_weight;
+    a->max_depth = c->max_depth;
+    a->min_z = c->min_z;
+    a->width = c->width;
+    a->height = c->height;
+    a->nframes = nframes;
+    a->dtype = c->dtype;
+    return GBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, uint16_t* counts, const void* depth,
+                            int32_t nframes, const void* rot, const void* trans, uint32_t* signature, void* stream) {
+    gbt::DiffArgs a;
+    gbt_status st = diff_args(cfg, nframes, &a);
+    if (st != GBT_OK) return st;
+    if (!tsdf || !weights || !counts || !depth || !rot || !trans)
+        return fail(GBT_ERR_INVALID_ARG, "gbt_diff_forward: NULL tensor");
+    a.D = tsdf;
+    a.W = weights;
+    a.count = counts;
+    a.signature = signature;
+    a.depth = depth;
+    a.rot = rot;
+    a.trans = trans;
+    cudaGetLastError();
+    cudaError_t e = gbt::launch_diff_forward(a, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "differentiable forward");
+    return GBT_OK;
+}
+
+gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
+                             const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
+                             const void* trans, void* grad_depth, double* grad_pose, void* stream) {
+    gbt::DiffArgs a;
+    gbt_status st = diff_args(cfg, nframes, &a);
+    if (st != GBT_OK) return st;
+    if (!grad_tsdf || !weights_before || !counts || !depth || !rot || !trans || !grad_depth || !grad_pose)
+        return fail(GBT_ERR_INVALID_ARG, "gbt_diff_backward: NULL tensor");
+    a.grad_D = grad_tsdf;
+    a.W = const_cast<void*>(weights_before);
+    a.count = const_cast<uint16_t*>(counts);
+    a.depth = depth;
+    a.rot = rot;
+    a.trans = trans;
+    a.grad_depth = grad_depth;
+    a.grad_pose = grad_pose;
+    cudaGetLastError();
+    cudaError_t e = gbt::launch_diff_backward(a, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "differentiable backward");
+    return GBT_OK;
+}
+
+}  // extern "C"

@@ -118,6 +118,26 @@ struct McArgs {
     int* error;                  // set to 1 when a look-back wait gives up
 };
 
+// Differentiable integrate (k_diff.cu).  dtype 0: float, 1: double for the
+// volume, depth, rotations, translations and depth gradient.
+struct DiffArgs {
+    int32_t nx, ny, nz;
+    float vs[3], off[3];
+    float fx, fy, cx, cy;
+    float trunc, max_weight, max_depth, min_z;
+    int32_t width, height, nframes, dtype;
+    void* D;                 // forward: in/out distances
+    void* W;                 // forward: in/out weights; backward: weights before the forward
+    uint16_t* count;         // updates per voxel (forward writes, backward reads)
+    uint32_t* signature;     // optional: hash of the discrete decisions per voxel
+    const void* depth;       // [nframes][height][width]
+    const void* rot;         // [nframes][9] row-major, world to camera
+    const void* trans;       // [nframes][3]
+    const void* grad_D;      // backward: dL/dD_final per voxel
+    void* grad_depth;        // backward: accumulated dL/ddepth
+    double* grad_pose;       // backward: accumulated [nframes][12] = dL/dR, dL/dt
+};
+
 // Launchers exported by the kernel translation units.
 // k_ref.cu (-use_fast_math): compat mode in the reference's arithmetic.
 cudaError_t launch_integrate_compat_ref(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
@@ -134,6 +154,9 @@ cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStre
 // k_util.cu: volume initialisation and the packed per-voxel transform records.
 cudaError_t launch_volume_init(float* D, float* W, int64_t n, float trunc, cudaStream_t s);
 cudaError_t launch_tvoxels(void* out, const VolDesc& v, cudaStream_t s);
+
+cudaError_t launch_diff_forward(const DiffArgs& a, cudaStream_t s);
+cudaError_t launch_diff_backward(const DiffArgs& a, cudaStream_t s);
 
 // Read-only views of a volume for translation units other than capi.cu.
 const VolDesc* volume_desc(const gbt_volume* v);

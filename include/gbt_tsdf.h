@@ -178,6 +178,47 @@ gbt_status gbt_integrate_batch(gbt_batch* batch, const gbt_batch_item* items, in
                                int32_t nframes, int32_t frames_per_launch, int32_t brick, int32_t ctas_per_sm,
                                void* stream);
 
+/* Differentiable integrate.  No counterpart in the reference (its integrate
+ * is not differentiable); it follows the fixed mode with bilinear depth
+ * sampling so the volume is differentiable in each depth pixel and in each
+ * frame's pose:  c = R p + t, (u, v) = (fx c.x/z + cx, fy c.y/z + cy),
+ * d = bilinear(depth, u, v) over four valid pixels, sdf = d - z,
+ * tsdf = min(sdf, truncation), D += (tsdf - D)/(w + 1), w = min(w + 1, max_weight),
+ * for z > min_z, the 2x2 footprint inside the image, sdf >= -truncation.
+ *
+ * Tensors are caller-owned device arrays of `dtype` (0 float32, 1 float64):
+ * tsdf/weights [nz][ny][nx], depth [nframes][height][width] metres,
+ * rot [nframes][9] (row-major world-to-camera rotation), trans [nframes][3].
+ * nframes <= GBT_MAX_FRAMES_PER_SCENE_PASS per call. */
+typedef struct {
+    uint32_t voxel_grid_size[3];
+    float voxel_size[3];
+    float global_offset[3];
+    float focal_x, focal_y, cx, cy;
+    float truncation;        /* > 0 */
+    float max_weight;        /* >= 1 */
+    float max_depth;         /* > 0 */
+    float min_z;
+    int32_t width, height;   /* depth image size */
+    int32_t dtype;           /* 0 float32, 1 float64 */
+} gbt_diff_cfg;
+
+/* Forward: updates tsdf/weights in place and writes counts[v], the number of
+ * updates voxel v received.  signature (optional, NULL) receives a per-voxel
+ * hash of the discrete decisions (validity, truncation, pixel cell): voxels
+ * whose hash changes between two poses are not smooth between them. */
+gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, uint16_t* counts, const void* depth,
+                            int32_t nframes, const void* rot, const void* trans, uint32_t* signature, void* stream);
+
+/* Adjoint of gbt_diff_forward for a gradient dL/dtsdf of the final distances:
+ * adds dL/ddepth into grad_depth ([nframes][height][width], dtype) and
+ * dL/dR, dL/dt into grad_pose ([nframes][12] float64: 9 row-major, then 3).
+ * weights_before are the weights the forward started from; counts are the
+ * forward's.  Recomputes each voxel-frame once; stores nothing per frame. */
+gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
+                             const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
+                             const void* trans, void* grad_depth, double* grad_pose, void* stream);
+
 /* Replaces generate_triangular_surface (marching_cubes.cu:191-237).
  * Writes up to cap_tris triangles: verts gets 9 floats per triangle (three
  * vertices, no sharing, as the reference emits them) and tris gets 3 ints per

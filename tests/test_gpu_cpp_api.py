@@ -70,8 +70,9 @@ def euler_pose(roll, yaw, pitch, t):
         return np.array([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
                          w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2])
     c = np.float32(np.pi / 180.0)
-    q = qmul(qmul(aa(np.float32(roll) * c, (0, 0, 1)), aa(np.float32(yaw) * c, (0, 1, 0))),
-             aa(np.float32(pitch) * c, (1, 0, 0)))
+    # degrees * (pi/180) is a float product (the factor is a float constant), the rest is double
+    ang = [float(np.float32(x) * c) for x in (roll, yaw, pitch)]
+    q = qmul(qmul(aa(ang[0], (0, 0, 1)), aa(ang[1], (0, 1, 0))), aa(ang[2], (1, 0, 0)))
     q /= np.linalg.norm(q)
     R = S.matrix_from_quat(q)
     q2 = S.quat_from_matrix(R)
@@ -91,7 +92,7 @@ def test_headless_example_matches_python_api(gpu, tmp_path, euler):
                  "tsdf.volume.camera.pose.euler.pitch: %r\ntsdf.volume.camera.pose.translation.x: %r\n"
                  "tsdf.volume.camera.pose.translation.y: %r\ntsdf.volume.camera.pose.translation.z: %r\n"
                  % (euler + t))
-        pose = euler_pose(*euler, t=[np.float32(x) for x in t])
+        pose = euler_pose(*euler, t=[float(np.float32(x)) for x in t])
     else:
         pose = np.array([1.0, 0, 0, 0, 0, 0, 0])
     ply = str(tmp_path / "mesh.ply")
