@@ -695,7 +695,8 @@ gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, 
 
 gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
                              const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
-                             const void* trans, void* grad_depth, double* grad_pose, void* stream) {
+                             const void* trans, void* grad_depth, double* grad_pose, void* grad_tsdf_before,
+                             void* stream) {
     gbt::DiffArgs a;
     gbt_status st = diff_args(cfg, nframes, &a);
     if (st != GBT_OK) return st;
@@ -709,6 +710,7 @@ gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, con
     a.trans = trans;
     a.grad_depth = grad_depth;
     a.grad_pose = grad_pose;
+    a.grad_D0 = grad_tsdf_before;
     cudaGetLastError();
     cudaError_t e = gbt::launch_diff_backward(a, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "differentiable backward");

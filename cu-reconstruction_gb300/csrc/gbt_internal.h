@@ -136,6 +136,7 @@ struct DiffArgs {
     const void* grad_D;      // backward: dL/dD_final per voxel
     void* grad_depth;        // backward: accumulated dL/ddepth
     double* grad_pose;       // backward: accumulated [nframes][12] = dL/dR, dL/dt
+    void* grad_D0;           // backward, optional: dL/dD before the forward
 };
 
 // Launchers exported by the kernel translation units.

@@ -138,6 +138,19 @@ __device__ __forceinline__ T beta(int m, int n, T w0, T M) {
     return O::mul(am, p);
 }
 
+// prod_{j=1..n} (1 - a_j): how much of the starting distance survives n updates.
+template <typename T>
+__device__ __forceinline__ T carry(int n, T w0, T M) {
+    using O = Ops<T>;
+    if (n == 0) return (T)1;
+    const T jsf = M - w0 + (T)1;
+    const int js = jsf < (T)1 ? 1 : (jsf > (T)(n + 1) ? n + 1 : (int)jsf);
+    const int jt = min(n, js - 1);
+    T p = jt >= 1 ? O::div(w0, O::add(w0, (T)jt)) : (T)1;
+    if (n >= js) p = O::mul(p, O::pow_(O::div(M, O::add(M, (T)1)), (T)(n - js + 1)));
+    return p;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) forward_kernel(Geometry g, T* D, T* W, uint16_t* count, uint32_t* signature,
                                                       const T* depth, const T* rot, const T* trans) {
@@ -186,7 +199,7 @@ __global__ void __launch_bounds__(256) forward_kernel(Geometry g, T* D, T* W, ui
 template <typename T>
 __global__ void __launch_bounds__(256) backward_kernel(Geometry g, const T* grad_D, const T* W0, const uint16_t* count,
                                                        const T* depth, const T* rot, const T* trans, T* grad_depth,
-                                                       double* grad_pose) {
+                                                       double* grad_pose, T* grad_D0) {
     __shared__ T s_pose[kBatchMaxFrames][12];
     __shared__ double s_acc[kBatchMaxFrames][12];
     using O = Ops<T>;
@@ -220,9 +233,10 @@ __global__ void __launch_bounds__(256) backward_kernel(Geometry g, const T* grad
             py = voxel_centre<T>(y, g.vs[1], g.off[1]);
             pz = voxel_centre<T>(z, g.vs[2], g.off[2]);
         }
+        w0 = w0 < (T)0 ? (T)0 : (w0 > (T)g.max_weight ? (T)g.max_weight : w0);
+        if (grad_D0 && inside) grad_D0[i] = O::mul(gD, carry<T>(nupd, w0, (T)g.max_weight));
         const bool active = inside && gD != (T)0 && nupd > 0;
         if (!__any_sync(0xffffffffu, active)) continue;
-        w0 = w0 < (T)0 ? (T)0 : (w0 > (T)g.max_weight ? (T)g.max_weight : w0);
         int m = 0;
         for (int f = 0; f < g.nframes; ++f) {
             const T* R = s_pose[f];
@@ -335,11 +349,11 @@ cudaError_t launch_diff_backward(const DiffArgs& a, cudaStream_t s) {
     if (a.dtype == 1) {
         diff::backward_kernel<double><<<diff::grid_for(n), 256, 0, s>>>(
             diff::geometry<double>(a), (const double*)a.grad_D, (const double*)a.W, a.count, (const double*)a.depth,
-            (const double*)a.rot, (const double*)a.trans, (double*)a.grad_depth, a.grad_pose);
+            (const double*)a.rot, (const double*)a.trans, (double*)a.grad_depth, a.grad_pose, (double*)a.grad_D0);
     } else {
         diff::backward_kernel<float><<<diff::grid_for(n), 256, 0, s>>>(
             diff::geometry<float>(a), (const float*)a.grad_D, (const float*)a.W, a.count, (const float*)a.depth,
-            (const float*)a.rot, (const float*)a.trans, (float*)a.grad_depth, a.grad_pose);
+            (const float*)a.rot, (const float*)a.trans, (float*)a.grad_depth, a.grad_pose, (float*)a.grad_D0);
     }
     return cudaGetLastError();
 }

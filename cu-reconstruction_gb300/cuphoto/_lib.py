@@ -73,6 +73,18 @@ class Frame(C.Structure):
     ]
 
 
+class DiffCfg(C.Structure):
+    _fields_ = [
+        ("voxel_grid_size", C.c_uint32 * 3),
+        ("voxel_size", C.c_float * 3),
+        ("global_offset", C.c_float * 3),
+        ("focal_x", C.c_float), ("focal_y", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+        ("truncation", C.c_float), ("max_weight", C.c_float), ("max_depth", C.c_float), ("min_z", C.c_float),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("dtype", C.c_int32),
+    ]
+
+
 class BatchItem(C.Structure):
     _fields_ = [("volume", C.c_void_p), ("first_frame", C.c_int32), ("nframes", C.c_int32)]
 
@@ -92,6 +104,10 @@ SIGNATURES = [
     ("gbt_batch_destroy", C.c_int, [C.c_void_p]),
     ("gbt_integrate_batch", C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int32, C.POINTER(Frame), C.c_int32,
                                       C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    ("gbt_diff_forward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("gbt_diff_backward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("gbt_extract_mesh", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                    C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,

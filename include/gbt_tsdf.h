@@ -212,12 +212,15 @@ gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, 
 
 /* Adjoint of gbt_diff_forward for a gradient dL/dtsdf of the final distances:
  * adds dL/ddepth into grad_depth ([nframes][height][width], dtype) and
- * dL/dR, dL/dt into grad_pose ([nframes][12] float64: 9 row-major, then 3).
+ * dL/dR, dL/dt into grad_pose ([nframes][12] float64: 9 row-major, then 3),
+ * and writes dL/dtsdf of the distances before the forward into
+ * grad_tsdf_before when it is not NULL (for chaining calls).
  * weights_before are the weights the forward started from; counts are the
  * forward's.  Recomputes each voxel-frame once; stores nothing per frame. */
 gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
                              const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
-                             const void* trans, void* grad_depth, double* grad_pose, void* stream);
+                             const void* trans, void* grad_depth, double* grad_pose, void* grad_tsdf_before,
+                             void* stream);
 
 /* Replaces generate_triangular_surface (marching_cubes.cu:191-237).
  * Writes up to cap_tris triangles: verts gets 9 floats per triangle (three

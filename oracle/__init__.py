@@ -140,6 +140,66 @@ def mc_fixed(cfg, D, W, index_base=0, threads=0):
 
 
 # ---------------------------------------------------------------------------
+# Differentiable integrate
+
+class OracleDiffCfg(C.Structure):
+    _fields_ = [
+        ("grid", C.c_uint32 * 3),
+        ("vs", C.c_float * 3),
+        ("off", C.c_float * 3),
+        ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+        ("trunc", C.c_float), ("max_weight", C.c_float), ("max_depth", C.c_float), ("min_z", C.c_float),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("dtype", C.c_int32),
+    ]
+
+
+def diff_cfg(grid, vs, off, K, trunc, max_weight, max_depth, min_z, width, height, dtype):
+    c = OracleDiffCfg()
+    for i in range(3):
+        c.grid[i], c.vs[i], c.off[i] = int(grid[i]), float(vs[i]), float(off[i])
+    c.fx, c.fy, c.cx, c.cy = (float(k) for k in K)
+    c.trunc, c.max_weight, c.max_depth, c.min_z = float(trunc), float(max_weight), float(max_depth), float(min_z)
+    c.width, c.height, c.dtype = int(width), int(height), int(dtype)
+    return c
+
+
+def _diff_lib():
+    so = lib()
+    if not getattr(so, "_diff_ready", False):
+        vp = C.c_void_p
+        so.oracle_diff_forward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, vp, vp, C.c_int32, vp, vp, C.c_int32]
+        so.oracle_diff_backward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, C.c_int32, vp, vp, vp, vp]
+        so._diff_ready = True
+    return so
+
+
+def diff_forward(cfg, D, W, depth, rot, trans, threads=0):
+    """In place on D, W (float32 or float64 per cfg.dtype); returns (count, signature)."""
+    n = D.size
+    count = np.zeros(n, np.uint16)
+    sig = np.zeros(n, np.uint32)
+    depth = np.ascontiguousarray(depth)
+    rot = np.ascontiguousarray(rot)
+    trans = np.ascontiguousarray(trans)
+    _diff_lib().oracle_diff_forward(C.byref(cfg), _p(D), _p(W), _p(count), _p(sig), _p(depth), len(depth), _p(rot),
+                                    _p(trans), threads)
+    return count.reshape(D.shape), sig.reshape(D.shape)
+
+
+def diff_backward(cfg, grad_D, W0, depth, rot, trans):
+    """float64 gradient: (grad_depth [F,H,W], grad_pose [F,12])."""
+    depth = np.ascontiguousarray(depth, np.float64)
+    gdep = np.zeros(depth.shape, np.float64)
+    gpose = np.zeros((len(depth), 12), np.float64)
+    _diff_lib().oracle_diff_backward(C.byref(cfg), _p(np.ascontiguousarray(grad_D, np.float64)),
+                                     _p(np.ascontiguousarray(W0, np.float64)), _p(depth), len(depth),
+                                     _p(np.ascontiguousarray(rot, np.float64)),
+                                     _p(np.ascontiguousarray(trans, np.float64)), _p(gdep), _p(gpose))
+    return gdep, gpose
+
+
+# ---------------------------------------------------------------------------
 class RefHarness:
     """The reference's own kernels (compiled from its sources) driven with its
     host-side logic.  Needs a GPU and oracle/_ref/ref_tsdf.cubin."""

@@ -328,3 +328,74 @@ def test_oracle_against_reference_golden(oracle, path):
     tol = max(1e-5 * float(np.max(oracle.derive(c)[0])), 2 * float(np.spacing(np.float32(np.abs(V).max(initial=1)))))
     np.testing.assert_allclose(V, g["verts"], rtol=0, atol=tol)
     assert np.array_equal(T, g["tris"])
+
+
+# ---------------------------------------------------------------------------
+# Differentiable integrate: the oracle's FP64 gradient against FP64 central
+# differences, on voxels whose discrete decisions do not change in the step.
+import diffcase  # noqa: E402
+
+
+def _oracle_loss(oracle, case, R, t, depth, mask=None):
+    cfg = oracle.diff_cfg(case["grid"], case["vs"], case["off"], case["K"], case["trunc"], case["max_weight"],
+                          case["max_depth"], case["min_z"], case["width"], case["height"], 1)
+    shape = case["grid"][::-1]
+    D = np.full(shape, case["trunc"], np.float64)
+    W = np.zeros(shape, np.float64)
+    cnt, sig = oracle.diff_forward(cfg, D, W, depth.astype(np.float64), R.reshape(-1, 9), t)
+    m = np.ones(shape, bool) if mask is None else mask
+    L = float(np.sum((W * (D - case["gt"]) ** 2)[m]))
+    return L, D, W, sig, cfg
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_oracle_gradient_matches_fp64_central_differences(oracle, seed):
+    case = diffcase.make_case(seed=seed)
+    dphi, dt, ddep = diffcase.perturbation(case, seed=seed + 10, scale_rot=1.0, scale_t=1.0, scale_depth=1.0)
+    h = 1e-6
+    Rp, tp, dp = diffcase.perturbed(case, h, dphi, dt, ddep)
+    Rm, tm, dm = diffcase.perturbed(case, -h, dphi, dt, ddep)
+    _, _, _, sig_p, _ = _oracle_loss(oracle, case, Rp, tp, dp)
+    _, _, _, sig_m, _ = _oracle_loss(oracle, case, Rm, tm, dm)
+    L0, D, W, sig0, cfg = _oracle_loss(oracle, case, case["R"], case["t"], case["depth"])
+    mask = (sig_p == sig0) & (sig_m == sig0)
+    assert mask.mean() > 0.5 and (W[mask] > 0).sum() > 500
+    Lp = _oracle_loss(oracle, case, Rp, tp, dp, mask)[0]
+    Lm = _oracle_loss(oracle, case, Rm, tm, dm, mask)[0]
+    fd = (Lp - Lm) / (2 * h)
+    gD = 2 * W * (D - case["gt"]) * mask
+    gdep, gpose = oracle.diff_backward(cfg, gD, np.zeros_like(W), case["depth"], case["R"].reshape(-1, 9), case["t"])
+    an = diffcase.directional(gpose[:, :9].reshape(-1, 3, 3), gpose[:, 9:], gdep, case, dphi, dt, ddep)
+    assert abs(fd) > 1e-6
+    assert abs(an - fd) <= 1e-6 * abs(fd), (an, fd)
+
+
+def test_oracle_gradient_with_saturated_weights(oracle):
+    """Weights already at max_weight before the frames: the running mean is an
+    exponential average; the gradient still matches central differences."""
+    case = diffcase.make_case(seed=3, frames=4)
+    case["max_weight"] = 2.0
+    dphi, dt, ddep = diffcase.perturbation(case, seed=7)
+    h = 1e-6
+    shape = case["grid"][::-1]
+
+    def run(R, t, depth, mask=None):
+        cfg = oracle.diff_cfg(case["grid"], case["vs"], case["off"], case["K"], case["trunc"], case["max_weight"],
+                              case["max_depth"], case["min_z"], case["width"], case["height"], 1)
+        D = np.full(shape, 0.01, np.float64)
+        W = np.full(shape, 2.0, np.float64)
+        cnt, sig = oracle.diff_forward(cfg, D, W, depth, R.reshape(-1, 9), t)
+        m = np.ones(shape, bool) if mask is None else mask
+        return float(np.sum(((D - case["gt"]) ** 2)[m])), D, sig, cfg
+
+    Rp, tp, dp = diffcase.perturbed(case, h, dphi, dt, ddep)
+    Rm, tm, dm = diffcase.perturbed(case, -h, dphi, dt, ddep)
+    _, _, sp, _ = run(Rp, tp, dp)
+    _, _, sm, _ = run(Rm, tm, dm)
+    _, D, s0, cfg = run(case["R"], case["t"], case["depth"])
+    mask = (sp == s0) & (sm == s0)
+    fd = (run(Rp, tp, dp, mask)[0] - run(Rm, tm, dm, mask)[0]) / (2 * h)
+    gdep, gpose = oracle.diff_backward(cfg, 2 * (D - case["gt"]) * mask, np.full(shape, 2.0), case["depth"],
+                                       case["R"].reshape(-1, 9), case["t"])
+    an = diffcase.directional(gpose[:, :9].reshape(-1, 3, 3), gpose[:, 9:], gdep, case, dphi, dt, ddep)
+    assert abs(an - fd) <= 1e-6 * abs(fd), (an, fd)
