@@ -186,18 +186,26 @@ def test_autograd_pose_refinement_reduces_error(gpu):
     def pose_err(R, t):
         return float((t - t_true).norm(dim=1).mean().item())
 
-    L0, _ = loss_and_grad(R, t)
-    e0 = pose_err(R, t)
-    step = None
-    for it in range(12):
-        L, g = loss_and_grad(R, t)
-        if step is None:
-            step = 1e-3 / max(g.abs().max().item(), 1e-30)
-        xi = -step * g
+    def apply(R, t, xi):
+        R2, t2 = R.clone(), t.clone()
         for k in range(R.shape[0]):
             dR = gpu.as_tensor(diffcase.rot_exp(xi[k, 3:].cpu().numpy()), device="cuda", dtype=dt)
-            R[k] = dR @ R[k]
-            t[k] = dR @ t[k] + xi[k, :3].to(dt)
-    L1, _ = loss_and_grad(R, t)
-    assert L1 < L0
+            R2[k] = dR @ R[k]
+            t2[k] = dR @ t[k] + xi[k, :3].to(dt)
+        return R2, t2
+
+    L0, g = loss_and_grad(R, t)
+    e0 = pose_err(R, t)
+    L = L0
+    step = 2e-3 / max(g.abs().max().item(), 1e-30)
+    for it in range(10):   # gradient steps with backtracking on the loss
+        while step * g.abs().max().item() > 1e-7:
+            R2, t2 = apply(R, t, -step * g)
+            L2, g2 = loss_and_grad(R2, t2)
+            if L2 < L:
+                R, t, L, g = R2, t2, L2, g2
+                step *= 1.5
+                break
+            step *= 0.5
+    assert L < 0.9 * L0
     assert pose_err(R, t) < e0
