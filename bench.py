@@ -44,8 +44,9 @@ def parse():
     ap.add_argument("--frames", type=int, default=300)
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene"],
-                    help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames")
+    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff"],
+                    help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames; "
+                         "diff: forward + adjoint timing and finite-difference check at 128^3 x 16 frames")
     return ap.parse_args()
 
 
@@ -179,6 +180,161 @@ def reference_cuda(args, cam, scene, poses, torch, nframes=8):
     wall = float(np.median([m[1] for m in ms]))
     return {"value": nvox / (kern * 1e-3), "unit": UNIT, "kernel_ms_per_frame": kern, "call_ms_per_frame": wall,
             "frames_timed": len(ms), "what": "TSDFVolume::integrate of the reference, one launch + sync per frame"}
+
+
+def differentiable_c3(torch, reps=20):
+    """Forward + adjoint of the differentiable integrate at 128^3, 16 frames
+    320x240 (FP32): CUDA-event times of the plain forward, the forward that
+    writes the adjoint's checkpoints and the adjoint, their ratio, and the
+    directional-derivative error of the FP64 and FP32 adjoints against FP64
+    central differences on the GPU (steps h and h/2, Richardson-extrapolated;
+    the plain step-h difference also given) along unit directions over all
+    poses (h = 1e-4 and 1e-5) and over all valid depth pixels (h = 1e-4)."""
+    from cuphoto import diff as DF
+    from cuphoto import synthetic as S
+    case = S.diff_case_frontal(128, 16)
+    cfg = DF.DiffConfig(case["grid"], tuple(float(v) for v in case["vs"]), tuple(float(v) for v in case["off"]),
+                        *case["K"], truncation=case["trunc"], max_weight=case["max_weight"],
+                        max_depth=case["max_depth"], min_z=case["min_z"])
+    shape = case["grid"][::-1]
+    F = len(case["R"])
+
+    def inputs(R, t, dep, dt):
+        return [torch.as_tensor(np.ascontiguousarray(x), device="cuda", dtype=dt) for x in (dep, R.reshape(-1, 9), t)]
+
+    def forward(R, t, dep, dt, ckpt=False, sig=False):
+        D = torch.full(shape, case["trunc"], dtype=dt, device="cuda")
+        W = torch.zeros(shape, dtype=dt, device="cuda")
+        ck = torch.empty(DF.checkpoint_shape(F, shape), dtype=dt, device="cuda") if ckpt else None
+        sg = torch.empty(shape, dtype=torch.int32, device="cuda") if sig else None
+        a = inputs(R, t, dep, dt)
+        DF.forward_raw(cfg, D, W, *a, ck, sg)
+        return D, W, ck, sg, a
+
+    def adjoint(D, W, ck, a, mask, dt):
+        gt = torch.as_tensor(case["gt"], device="cuda", dtype=dt)
+        gD = (2 * W * (D - gt) * mask).contiguous()
+        gW = ((D - gt) ** 2 * mask).contiguous()
+        D0 = torch.full(shape, case["trunc"], dtype=dt, device="cuda")
+        W0 = torch.zeros(shape, dtype=dt, device="cuda")
+        gdep = torch.zeros_like(a[0])
+        gpose = torch.zeros((F, 12), dtype=torch.float64, device="cuda")
+        return (gD, gW, D0, W0, gdep, gpose), lambda: DF.backward_raw(cfg, gD, gW, D0, W0, ck, *a, gdep, gpose)
+
+    # timing, FP32
+    R32, t32, dep32 = case["R"], case["t"], case["depth"]
+    D, W, ck, _, a = forward(R32, t32, dep32, torch.float32, ckpt=True)
+    bufs, run_adj = adjoint(D, W, ck, a, torch.ones(shape, dtype=torch.bool, device="cuda"), torch.float32)
+    Dp = torch.empty_like(D)
+    Wp = torch.empty_like(W)
+
+    def fwd_plain():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+        DF.forward_raw(cfg, Dp, Wp, *a)
+
+    def fwd_ckpt():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+        DF.forward_raw(cfg, Dp, Wp, *a, ck)
+
+    def fill_only():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+
+    def adj():
+        bufs[4].zero_()
+        bufs[5].zero_()
+        run_adj()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_fill = timed(fill_only)
+    t_plain = timed(fwd_plain) - t_fill
+    t_ckpt = timed(fwd_ckpt) - t_fill
+    t_adj = timed(adj) - timed(lambda: (bufs[4].zero_(), bufs[5].zero_()))
+    nvf = int(np.prod(shape)) * F
+
+    # FD check, FP64 on the GPU
+    def fd_check(which, h):
+        rng = np.random.default_rng(3)
+        dphi = rng.normal(size=(F, 3))
+        dtr = rng.normal(size=(F, 3))
+        ddep = rng.normal(size=case["depth"].shape) * (case["depth"] > 0)
+        if which == "pose":
+            ddep = ddep * 0
+        else:
+            dphi, dtr = dphi * 0, dtr * 0
+        nrm = np.sqrt((dphi ** 2).sum() + (dtr ** 2).sum() + (ddep ** 2).sum())
+        dphi, dtr, ddep = dphi / nrm, dtr / nrm, ddep / nrm
+
+        def perturbed(h):
+            R = np.stack([S.axis_angle_matrix(h * dphi[k]) @ case["R"][k] for k in range(F)])
+            return R, case["t"] + h * dtr, case["depth"] + h * ddep
+
+        runs = {k: perturbed(k * h) for k in (1, 0.5, -0.5, -1)}
+        D, W, ck, s0, a = forward(case["R"], case["t"], case["depth"], torch.float64, ckpt=True, sig=True)
+        mask = torch.ones(shape, dtype=torch.bool, device="cuda")
+        for k in runs:
+            mask &= forward(*runs[k], torch.float64, sig=True)[3] == s0
+        gt = torch.as_tensor(case["gt"], device="cuda", dtype=torch.float64)
+
+        def loss(k):
+            D2, W2 = forward(*runs[k], torch.float64)[:2]
+            return float((W2 * (D2 - gt) ** 2)[mask].sum().item())
+
+        L = {k: loss(k) for k in runs}
+        d1 = (L[1] - L[-1]) / (2 * h)
+        fd = (4 * (L[0.5] - L[-0.5]) / h - d1) / 3
+
+        def directional(dt):
+            Dx, Wx, ckx, _, ax = forward(case["R"], case["t"], case["depth"], dt, ckpt=True)
+            b, run = adjoint(Dx, Wx, ckx, ax, mask, dt)
+            run()
+            gdep, gpose = b[4].double().cpu().numpy(), b[5].cpu().numpy()
+            s = float(np.sum(gdep * ddep))
+            for k in range(F):
+                dR = np.cross(np.eye(3), dphi[k]) @ case["R"][k]   # hat(dphi) R
+                s += float(np.sum(gpose[k, :9].reshape(3, 3) * dR) + gpose[k, 9:] @ dtr[k])
+            return s
+
+        an64 = directional(torch.float64)
+        an32 = directional(torch.float32)
+        return {"step": h, "fd": fd, "fd_plain": d1, "adjoint_fp64": an64, "adjoint_fp32": an32,
+                "rel_err_fp64": abs(an64 - fd) / abs(fd), "rel_err_fp32": abs(an32 - fd) / abs(fd),
+                "rel_err_fp64_vs_plain_fd": abs(an64 - d1) / abs(d1),
+                "voxels_compared": float(mask.float().mean().item())}
+
+    def fp32_vs_fp64():
+        D64, W64, ck64, s64, a64 = forward(case["R"], case["t"], case["depth"], torch.float64, ckpt=True, sig=True)
+        D32, W32, ck32, s32, a32 = forward(case["R"], case["t"], case["depth"], torch.float32, ckpt=True, sig=True)
+        m = s32 == s64
+        b64, run64 = adjoint(D64, W64, ck64, a64, m, torch.float64)
+        b32, run32 = adjoint(D32, W32, ck32, a32, m, torch.float32)
+        run64()
+        run32()
+        rel = lambda x, y: float((x.double() - y).norm().item() / y.norm().item())
+        return {"voxels_same_decisions": float(m.float().mean().item()), "grad_depth_rel_l2": rel(b32[4], b64[4]),
+                "grad_pose_rel_l2": rel(b32[5], b64[5])}
+
+    return {"config": "128^3 voxels, 16 frames 320x240 float32 depth, frontal plane+spheres scene, "
+                      "L = sum W (D - sdf_gt)^2",
+            "forward_ms": t_plain, "forward_with_checkpoints_ms": t_ckpt, "adjoint_ms": t_adj,
+            "fwd_plus_adjoint_over_fwd": (t_ckpt + t_adj) / t_plain,
+            "forward_voxel_updates_per_s": nvf / (t_plain * 1e-3),
+            "fd_pose": [fd_check("pose", 1e-4), fd_check("pose", 1e-5)], "fd_depth": fd_check("depth", 1e-4),
+            "fp32_vs_fp64": fp32_vs_fp64()}
 
 
 def run_reference_arm(args):
@@ -385,6 +541,16 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args)
         return
+    if args.workload == "diff":
+        import torch
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+        eb = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(eb)
+        eb.build()
+        print(json.dumps({"workload": "differentiable integrate, 128^3 x 16 frames 320x240",
+                          "differentiable": differentiable_c3(torch)}), flush=True)
+        return
     if args.workload == "multiscene":
         import torch
         rank, world, local = dist_env()
@@ -548,6 +714,7 @@ def main():
     extras = {}
     if not args.no_extras and world == 1:
         extras["reference_cuda"] = reference_cuda(args, cam, scene, poses, torch)
+        extras["differentiable"] = differentiable_c3(torch)
         cpu = cpu_baseline(args, cam, scene, poses)
     else:
         cpu = None

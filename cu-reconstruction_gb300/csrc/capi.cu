@@ -641,8 +641,8 @@ gbt_status diff_args(const gbt_diff_cfg* c, int32_t nframes, gbt::DiffArgs* a) {
             return fail(GBT_ERR_INVALID_ARG, "grid/voxel size %d must be positive", i);
     const int64_t n = (int64_t)c->voxel_grid_size[0] * c->voxel_grid_size[1] * c->voxel_grid_size[2];
     if (n >= (int64_t)1 << 32) return fail(GBT_ERR_INVALID_ARG, "more than 2^32-1 voxels");
-    if (!(c->truncation > 0.f) || !(c->max_weight >= 1.f) || !(c->max_depth > 0.f))
-        return fail(GBT_ERR_INVALID_ARG, "truncation, max_depth must be > 0 and max_weight >= 1");
+    if (!(c->truncation > 0.f) || !(c->max_weight > 0.f) || !(c->max_depth > 0.f))
+        return fail(GBT_ERR_INVALID_ARG, "truncation, max_depth and max_weight must be > 0");
     if (c->width < 2 || c->height < 2) return fail(GBT_ERR_INVALID_ARG, "depth images need at least 2x2 pixels");
     if (nframes < 1 || nframes > GBT_MAX_FRAMES_PER_SCENE_PASS)
         return fail(GBT_ERR_INVALID_ARG, "nframes %d outside 1..%d", nframes, GBT_MAX_FRAMES_PER_SCENE_PASS);
@@ -673,16 +673,16 @@ gbt_status diff_args(const gbt_diff_cfg* c, int32_t nframes, gbt::DiffArgs* a) {
 
 extern "C" {
 
-gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, uint16_t* counts, const void* depth,
-                            int32_t nframes, const void* rot, const void* trans, uint32_t* signature, void* stream) {
+gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, void* checkpoints,
+                            uint32_t* signature, const void* depth, int32_t nframes, const void* rot,
+                            const void* trans, void* stream) {
     gbt::DiffArgs a;
     gbt_status st = diff_args(cfg, nframes, &a);
     if (st != GBT_OK) return st;
-    if (!tsdf || !weights || !counts || !depth || !rot || !trans)
-        return fail(GBT_ERR_INVALID_ARG, "gbt_diff_forward: NULL tensor");
+    if (!tsdf || !weights || !depth || !rot || !trans) return fail(GBT_ERR_INVALID_ARG, "gbt_diff_forward: NULL tensor");
     a.D = tsdf;
     a.W = weights;
-    a.count = counts;
+    a.ckpt = checkpoints;
     a.signature = signature;
     a.depth = depth;
     a.rot = rot;
@@ -693,24 +693,31 @@ gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, 
     return GBT_OK;
 }
 
-gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
-                             const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
-                             const void* trans, void* grad_depth, double* grad_pose, void* grad_tsdf_before,
-                             void* stream) {
+gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* grad_weights,
+                             const void* tsdf_before, const void* weights_before, const void* checkpoints,
+                             const void* depth, int32_t nframes, const void* rot, const void* trans,
+                             void* grad_depth, double* grad_pose, void* grad_tsdf_before,
+                             void* grad_weights_before, void* stream) {
     gbt::DiffArgs a;
     gbt_status st = diff_args(cfg, nframes, &a);
     if (st != GBT_OK) return st;
-    if (!grad_tsdf || !weights_before || !counts || !depth || !rot || !trans || !grad_depth || !grad_pose)
+    if (!grad_tsdf || !tsdf_before || !weights_before || !depth || !rot || !trans || !grad_depth || !grad_pose)
         return fail(GBT_ERR_INVALID_ARG, "gbt_diff_backward: NULL tensor");
+    if (nframes > GBT_DIFF_CHUNK_FRAMES && !checkpoints)
+        return fail(GBT_ERR_INVALID_ARG, "gbt_diff_backward: more than %d frames need the forward's checkpoints",
+                    GBT_DIFF_CHUNK_FRAMES);
     a.grad_D = grad_tsdf;
+    a.grad_W = grad_weights;
+    a.D = const_cast<void*>(tsdf_before);
     a.W = const_cast<void*>(weights_before);
-    a.count = const_cast<uint16_t*>(counts);
+    a.ckpt = const_cast<void*>(checkpoints);
     a.depth = depth;
     a.rot = rot;
     a.trans = trans;
     a.grad_depth = grad_depth;
     a.grad_pose = grad_pose;
     a.grad_D0 = grad_tsdf_before;
+    a.grad_W0 = grad_weights_before;
     cudaGetLastError();
     cudaError_t e = gbt::launch_diff_backward(a, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "differentiable backward");

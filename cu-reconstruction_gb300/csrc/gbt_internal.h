@@ -119,24 +119,27 @@ struct McArgs {
 };
 
 // Differentiable integrate (k_diff.cu).  dtype 0: float, 1: double for the
-// volume, depth, rotations, translations and depth gradient.
+// volume, depth, rotations and translations; gradients of depth and pose are
+// accumulated in double.
 struct DiffArgs {
     int32_t nx, ny, nz;
     float vs[3], off[3];
     float fx, fy, cx, cy;
     float trunc, max_weight, max_depth, min_z;
     int32_t width, height, nframes, dtype;
-    void* D;                 // forward: in/out distances
+    void* D;                 // forward: in/out distances; backward: distances before the forward
     void* W;                 // forward: in/out weights; backward: weights before the forward
-    uint16_t* count;         // updates per voxel (forward writes, backward reads)
-    uint32_t* signature;     // optional: hash of the discrete decisions per voxel
+    void* ckpt;              // (D, W) before every chunk after the first: [nchunks-1][2][N]
+    uint32_t* signature;     // forward, optional: hash of the discrete decisions per voxel
     const void* depth;       // [nframes][height][width]
     const void* rot;         // [nframes][9] row-major, world to camera
     const void* trans;       // [nframes][3]
-    const void* grad_D;      // backward: dL/dD_final per voxel
-    void* grad_depth;        // backward: accumulated dL/ddepth
+    const void* grad_D;      // backward: dL/dD_final
+    const void* grad_W;      // backward, optional: dL/dW_final
+    void* grad_depth;        // backward: accumulated dL/ddepth (dtype)
     double* grad_pose;       // backward: accumulated [nframes][12] = dL/dR, dL/dt
     void* grad_D0;           // backward, optional: dL/dD before the forward
+    void* grad_W0;           // backward, optional: dL/dW before the forward
 };
 
 // Launchers exported by the kernel translation units.

@@ -1,24 +1,30 @@
 // Differentiable integrate: forward and adjoint, in float and in double.
 //
-// The forward is the fixed mode's running average with bilinear depth
-// sampling, so the result is differentiable in the pose and in each depth
-// pixel:  c = R p + t,  (u, v) = (fx c.x / z + cx, fy c.y / z + cy),
-// d = bilinear(depth, u, v) (all four pixels valid), sdf = d - z,
-// tsdf = min(sdf, trunc), D += (tsdf - D) / (w + 1), w = min(w + 1, M).
-// A voxel-frame counts only with z > min_z, the 2x2 footprint inside the image
-// and sdf >= -trunc.  The forward also writes n, the number of updates each
-// voxel received.
+// Forward, per voxel and frame (fixed-mode geometry, bilinear depth):
+//   c = R p + t,  (u, v) = (fx c.x / z + cx, fy c.y / z + cy),
+//   the 2x2 footprint around (u, v) with bilinear weights b_i and validity
+//   v_i (pixel inside the image with depth in (0, max_depth]),
+//   wv = sum b_i v_i,  d = sum b_i v_i d_i / wv,  sdf = d - z,
+//   tsdf = min(sdf, trunc),  w = wv * ramp((sdf + trunc) / (trunc / 2)),
+//   ramp(x) = clamp(x, 0, 1), and for w > 0:
+//   D += w (tsdf - D) / (W + w),  W = min(W + w, M).
+// Every cut is soft: a sample's weight goes to zero continuously as its
+// footprint leaves the image or the valid depth, and at the back of the
+// truncation band, so D and W are continuous in the pose and in every depth
+// pixel (only z <= min_z is a hard cut).
 //
-// Adjoint.  The recurrence is linear in the updates: D_final =
-// prod(1 - a_j) D_0 + sum_m beta_m tsdf_m with a_j = 1 / (min(w0 + j - 1, M) + 1)
-// for the j-th update of the voxel and beta_m = a_m prod_{j>m} (1 - a_j); the
-// weights do not depend on the continuous inputs.  beta_m has a closed form in
-// (m, n, w0, M) -- 1 / (w0 + n) while the weight stays below M, a geometric
-// tail once it saturates -- so the adjoint recomputes each voxel-frame once, in
-// forward order, with no per-frame volumes stored: dL/dtsdf_m = g beta_m for
-// g = dL/dD_final, then through min(., trunc), the bilinear sample (scattered
-// to the four pixels of dL/ddepth) and the projection to dL/dR = sum g_c p^T,
-// dL/dt = sum g_c per frame (g_c = dL/dc).
+// Adjoint: reverse mode through the recurrence with frame-chunk
+// recomputation.  The forward writes (D, W) before every chunk of kChunk frames
+// after the first; the adjoint walks the chunks backwards, recomputes each
+// chunk forward from its checkpoint keeping the per-frame (D, W) in registers,
+// then runs the chunk in reverse: for each update
+//   dD_k/dD_{k-1} = W_{k-1}/(W_{k-1}+w),  dD_k/dtsdf = w/(W_{k-1}+w),
+//   dD_k/dw = (tsdf - D_{k-1}) W_{k-1}/(W_{k-1}+w)^2,
+//   dD_k/dW_{k-1} = -w (tsdf - D_{k-1})/(W_{k-1}+w)^2,
+//   dW_k/dW_{k-1} = dW_k/dw = 1 below the clamp, 0 at it,
+// then through min(., trunc), the ramp, the normalised bilinear sample
+// (scattered to the valid pixels of dL/ddepth) and the projection to
+// dL/dR = sum g_c p^T, dL/dt = sum g_c per frame.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -26,6 +32,8 @@
 
 namespace gbt {
 namespace diff {
+
+constexpr int kChunk = GBT_DIFF_CHUNK_FRAMES;
 
 template <typename T> struct Ops;
 
@@ -38,7 +46,6 @@ template <> struct Ops<float> {
     __device__ static float div(float a, float b) { return __fdiv_rn(a, b); }
     __device__ static float floor_(float a) { return floorf(a); }
     __device__ static float min_(float a, float b) { return fminf(a, b); }
-    __device__ static float pow_(float a, float e) { return powf(a, e); }
 };
 
 template <> struct Ops<double> {
@@ -50,7 +57,6 @@ template <> struct Ops<double> {
     __device__ static double div(double a, double b) { return __ddiv_rn(a, b); }
     __device__ static double floor_(double a) { return floor(a); }
     __device__ static double min_(double a, double b) { return fmin(a, b); }
-    __device__ static double pow_(double a, double e) { return pow(a, e); }
 };
 
 struct Geometry {
@@ -62,16 +68,17 @@ struct Geometry {
     int32_t nframes;
 };
 
-// Everything the forward and the adjoint need about one voxel-frame.
+// One voxel-frame.  band: 0 = weight 0, 1 = inside the ramp, 2 = full.
 template <typename T> struct Sample {
-    bool valid;
-    bool truncated;      // sdf > trunc: tsdf = trunc, no gradient
+    bool truncated;      // sdf > trunc
+    int band;
     int u0, v0;
-    T a, b;              // bilinear fractions
-    T d00, d10, d01, d11;
-    T cx, cy, cz;        // camera coordinates
-    T rz;
-    T sdf, tsdf;
+    int vmask;           // bit i: pixel i of the footprint is valid (00, 10, 01, 11)
+    T a, b;
+    T d[4];
+    T wv, dn;            // valid bilinear weight, normalised depth
+    T cx, cy, cz, rz;
+    T sdf, tsdf, wband, w;
 };
 
 template <typename T>
@@ -81,10 +88,25 @@ __device__ __forceinline__ T voxel_centre(int v, float vs, float off) {
 }
 
 template <typename T>
+__device__ __forceinline__ T ramp(T x, int* state) {
+    if (!(x > (T)0)) {
+        *state = 0;
+        return (T)0;
+    }
+    if (x >= (T)1) {
+        *state = 2;
+        return (T)1;
+    }
+    *state = 1;
+    return x;
+}
+
+template <typename T>
 __device__ __forceinline__ void sample(const Geometry& g, const T* R, const T* t, const T* depth, T px, T py, T pz,
                                        Sample<T>& s) {
     using O = Ops<T>;
-    s.valid = false;
+    s.w = (T)0;
+    s.vmask = 0;
     s.cz = O::add(O::fma(R[8], pz, O::fma(R[6], px, O::mul(R[7], py))), t[2]);
     if (!(s.cz > (T)g.min_z)) return;
     s.cx = O::add(O::fma(R[2], pz, O::fma(R[0], px, O::mul(R[1], py))), t[0]);
@@ -92,211 +114,277 @@ __device__ __forceinline__ void sample(const Geometry& g, const T* R, const T* t
     s.rz = O::rcp(s.cz);
     const T u = O::fma((T)g.fx, O::mul(s.cx, s.rz), (T)g.cx);
     const T v = O::fma((T)g.fy, O::mul(s.cy, s.rz), (T)g.cy);
-    if (!(u >= (T)0 && v >= (T)0 && u < (T)(g.width - 1) && v < (T)(g.height - 1))) return;
+    if (!(u > (T)-1 && v > (T)-1 && u < (T)g.width && v < (T)g.height)) return;
     const T fu = O::floor_(u), fv = O::floor_(v);
     s.u0 = (int)fu;
     s.v0 = (int)fv;
     s.a = O::sub(u, fu);
     s.b = O::sub(v, fv);
-    const T* row0 = depth + (int64_t)s.v0 * g.width + s.u0;
-    const T* row1 = row0 + g.width;
-    s.d00 = row0[0];
-    s.d10 = row0[1];
-    s.d01 = row1[0];
-    s.d11 = row1[1];
     const T md = (T)g.max_depth;
-    if (!(s.d00 > (T)0 && s.d10 > (T)0 && s.d01 > (T)0 && s.d11 > (T)0 && s.d00 <= md && s.d10 <= md &&
-          s.d01 <= md && s.d11 <= md))
-        return;
-    const T top = O::fma(s.a, O::sub(s.d10, s.d00), s.d00);
-    const T bot = O::fma(s.a, O::sub(s.d11, s.d01), s.d01);
-    const T d = O::fma(s.b, O::sub(bot, top), top);
-    s.sdf = O::sub(d, s.cz);
-    if (!(s.sdf >= -(T)g.trunc)) return;
-    s.truncated = s.sdf > (T)g.trunc;
-    s.tsdf = O::min_(s.sdf, (T)g.trunc);
-    s.valid = true;
-}
-
-// Coefficient of the m-th (1-based) of n updates of a voxel whose weight was
-// w0 before the first, weights clamped at M:  a_j = 1 / (min(w0 + j - 1, M) + 1),
-// beta_m = a_m prod_{j=m+1..n} (1 - a_j).
-template <typename T>
-__device__ __forceinline__ T beta(int m, int n, T w0, T M) {
-    using O = Ops<T>;
-    // updates j < js see an unsaturated weight w0 + j - 1 < M
-    const T jsf = M - w0 + (T)1;
-    const int js = jsf < (T)1 ? 1 : (jsf > (T)(n + 1) ? n + 1 : (int)jsf);
-    const T r = O::div(M, O::add(M, (T)1));
-    const T am = m < js ? O::rcp(O::add(w0, (T)m)) : O::rcp(O::add(M, (T)1));
-    // telescoping part over j in [m+1, min(n, js-1)]: (w0 + m) / (w0 + min(n, js-1))
-    const int jt = min(n, js - 1);
-    T p = (T)1;
-    if (m + 1 <= jt) p = O::div(O::add(w0, (T)m), O::add(w0, (T)jt));
-    const int lo = max(m + 1, js);
-    if (n >= lo) p = O::mul(p, O::pow_(r, (T)(n - lo + 1)));
-    return O::mul(am, p);
-}
-
-// prod_{j=1..n} (1 - a_j): how much of the starting distance survives n updates.
-template <typename T>
-__device__ __forceinline__ T carry(int n, T w0, T M) {
-    using O = Ops<T>;
-    if (n == 0) return (T)1;
-    const T jsf = M - w0 + (T)1;
-    const int js = jsf < (T)1 ? 1 : (jsf > (T)(n + 1) ? n + 1 : (int)jsf);
-    const int jt = min(n, js - 1);
-    T p = jt >= 1 ? O::div(w0, O::add(w0, (T)jt)) : (T)1;
-    if (n >= js) p = O::mul(p, O::pow_(O::div(M, O::add(M, (T)1)), (T)(n - js + 1)));
-    return p;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = s.u0 + (k & 1), y = s.v0 + (k >> 1);
+        T dv = (T)0;
+        if (x >= 0 && y >= 0 && x < g.width && y < g.height) dv = depth[(int64_t)y * g.width + x];
+        s.d[k] = dv;
+        if (dv > (T)0 && dv <= md) s.vmask |= 1 << k;
+    }
+    if (!s.vmask) return;
+    const T ia = O::sub((T)1, s.a), ib = O::sub((T)1, s.b);
+    const T bw[4] = {O::mul(ia, ib), O::mul(s.a, ib), O::mul(ia, s.b), O::mul(s.a, s.b)};
+    T wv = (T)0, nd = (T)0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (s.vmask & (1 << k)) {
+            wv = O::add(wv, bw[k]);
+            nd = O::fma(bw[k], s.d[k], nd);
+        }
+    s.wv = wv;
+    if (!(wv > (T)0)) return;
+    s.dn = O::div(nd, wv);
+    s.sdf = O::sub(s.dn, s.cz);
+    const T tr = (T)g.trunc;
+    s.truncated = s.sdf > tr;
+    s.tsdf = O::min_(s.sdf, tr);
+    s.wband = ramp<T>(O::mul(O::add(s.sdf, tr), O::div((T)2, tr)), &s.band);
+    s.w = O::mul(s.wv, s.wband);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) forward_kernel(Geometry g, T* D, T* W, uint16_t* count, uint32_t* signature,
-                                                      const T* depth, const T* rot, const T* trans) {
-    __shared__ T s_pose[kBatchMaxFrames][12];
-    using O = Ops<T>;
+__device__ __forceinline__ uint32_t decision_code(const Sample<T>& s, bool saturated) {
+    if (!(s.w > (T)0)) return 0x7fffffffu;
+    return ((uint32_t)(s.u0 * 4099 + s.v0 * 7) ^ ((uint32_t)s.band << 24) ^ ((uint32_t)s.vmask << 26) ^
+            (s.truncated ? 0x80000000u : 0u) ^ (saturated ? 0x40000000u : 0u));
+}
+
+template <typename T>
+__device__ __forceinline__ void load_poses(const Geometry& g, const T* rot, const T* trans, T (*s_pose)[12]) {
     for (int f = threadIdx.x; f < g.nframes; f += blockDim.x) {
         for (int k = 0; k < 9; ++k) s_pose[f][k] = rot[9 * f + k];
         for (int k = 0; k < 3; ++k) s_pose[f][9 + k] = trans[3 * f + k];
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void voxel_xyz(const Geometry& g, int64_t i, T* px, T* py, T* pz) {
+    const int x = (int)(i % g.nx);
+    const int64_t r = i / g.nx;
+    const int y = (int)(r % g.ny), z = (int)(r / g.ny);
+    *px = voxel_centre<T>(x, g.vs[0], g.off[0]);
+    *py = voxel_centre<T>(y, g.vs[1], g.off[1]);
+    *pz = voxel_centre<T>(z, g.vs[2], g.off[2]);
+}
+
+// One update of the running mean; returns whether the weight clamp was reached.
+template <typename T>
+__device__ __forceinline__ bool update(T& d, T& w, const Sample<T>& s, T M) {
+    using O = Ops<T>;
+    const T sw = O::add(w, s.w);
+    d = O::fma(s.w, O::div(O::sub(s.tsdf, d), sw), d);
+    const bool sat = !(sw < M);
+    w = sat ? M : sw;
+    return sat;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) forward_kernel(Geometry g, T* D, T* W, T* ckpt, uint32_t* signature,
+                                                      const T* depth, const T* rot, const T* trans) {
+    __shared__ T s_pose[kBatchMaxFrames][12];
+    load_poses<T>(g, rot, trans, s_pose);
     __syncthreads();
     const int64_t n = (int64_t)g.nx * g.ny * g.nz;
     const int64_t frame = (int64_t)g.width * g.height;
+    const T M = (T)g.max_weight;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(i % g.nx);
-        const int64_t r = i / g.nx;
-        const int y = (int)(r % g.ny), z = (int)(r / g.ny);
-        const T px = voxel_centre<T>(x, g.vs[0], g.off[0]);
-        const T py = voxel_centre<T>(y, g.vs[1], g.off[1]);
-        const T pz = voxel_centre<T>(z, g.vs[2], g.off[2]);
+        T px, py, pz;
+        voxel_xyz<T>(g, i, &px, &py, &pz);
         T d = D[i], w = W[i];
-        int cnt = 0;
         uint32_t sig = 2166136261u;
         for (int f = 0; f < g.nframes; ++f) {
+            if (f > 0 && f % kChunk == 0 && ckpt) {
+                T* c = ckpt + (int64_t)(f / kChunk - 1) * 2 * n;
+                c[i] = d;
+                c[n + i] = w;
+            }
             Sample<T> s;
             sample<T>(g, s_pose[f], s_pose[f] + 9, depth + f * frame, px, py, pz, s);
-            if (signature) {
-                const uint32_t code = s.valid ? (uint32_t)(s.u0 * 4099 + s.v0 * 7) ^ (s.truncated ? 0x80000000u : 0u)
-                                              : 0x7fffffffu;
-                sig = (sig ^ code) * 16777619u;
-            }
-            if (!s.valid) continue;
-            const T inv = O::rcp(O::add(w, (T)1));
-            d = O::fma(O::sub(s.tsdf, d), inv, d);
-            w = O::min_(O::add(w, (T)1), (T)g.max_weight);
-            ++cnt;
+            bool sat = false;
+            if (s.w > (T)0) sat = update<T>(d, w, s, M);
+            if (signature) sig = (sig ^ decision_code<T>(s, sat)) * 16777619u;
         }
         D[i] = d;
         W[i] = w;
-        count[i] = (uint16_t)cnt;
         if (signature) signature[i] = sig;
     }
 }
 
-// grad_pose: [nframes][12] doubles (dL/dR row-major, dL/dt), accumulated.
-// grad_depth: [nframes][H][W], accumulated.
+// Sums 12 per-lane values over the warp with a transposing butterfly: each
+// of the five exchange rounds halves the values a lane keeps (16 -> 8 -> 4 ->
+// 2 -> 1, the 12 padded to 16), 16 shuffles in all instead of 12 x 5.  On
+// return, even lanes 0, 2, ..., 22 hold the warp total of value lane / 2.
 template <typename T>
-__global__ void __launch_bounds__(256) backward_kernel(Geometry g, const T* grad_D, const T* W0, const uint16_t* count,
-                                                       const T* depth, const T* rot, const T* trans, T* grad_depth,
-                                                       double* grad_pose, T* grad_D0) {
-    __shared__ T s_pose[kBatchMaxFrames][12];
-    __shared__ double s_acc[kBatchMaxFrames][12];
-    using O = Ops<T>;
-    for (int f = threadIdx.x; f < g.nframes; f += blockDim.x) {
-        for (int k = 0; k < 9; ++k) s_pose[f][k] = rot[9 * f + k];
-        for (int k = 0; k < 3; ++k) s_pose[f][9 + k] = trans[3 * f + k];
-        for (int k = 0; k < 12; ++k) s_acc[f][k] = 0.0;
-    }
-    __syncthreads();
-    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
-    const int64_t frame = (int64_t)g.width * g.height;
-    const int lane = threadIdx.x & 31;
-    // whole warps stay in the loop so the per-frame warp reductions see every lane
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t start = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t warp_first = start - lane;
-    for (int64_t i0 = warp_first; i0 < n; i0 += stride) {
-        const int64_t i = i0 + lane;
-        const bool inside = i < n;
-        T gD = (T)0, w0 = (T)0;
-        int nupd = 0;
-        T px = 0, py = 0, pz = 0;
-        if (inside) {
-            gD = grad_D[i];
-            w0 = W0[i];
-            nupd = count[i];
-            const int x = (int)(i % g.nx);
-            const int64_t r = i / g.nx;
-            const int y = (int)(r % g.ny), z = (int)(r / g.ny);
-            px = voxel_centre<T>(x, g.vs[0], g.off[0]);
-            py = voxel_centre<T>(y, g.vs[1], g.off[1]);
-            pz = voxel_centre<T>(z, g.vs[2], g.off[2]);
-        }
-        w0 = w0 < (T)0 ? (T)0 : (w0 > (T)g.max_weight ? (T)g.max_weight : w0);
-        if (grad_D0 && inside) grad_D0[i] = O::mul(gD, carry<T>(nupd, w0, (T)g.max_weight));
-        const bool active = inside && gD != (T)0 && nupd > 0;
-        if (!__any_sync(0xffffffffu, active)) continue;
-        int m = 0;
-        for (int f = 0; f < g.nframes; ++f) {
-            const T* R = s_pose[f];
-            T acc[12];
-            bool any = false;
+__device__ __forceinline__ T warp_sum12(const T (&acc)[12], int lane) {
+    T v[16];
 #pragma unroll
-            for (int k = 0; k < 12; ++k) acc[k] = (T)0;
+    for (int q = 0; q < 16; ++q) v[q] = q < 12 ? acc[q] : (T)0;
+#pragma unroll
+    for (int half = 8; half >= 1; half >>= 1) {
+        const bool hi = (lane & (2 * half)) != 0;   // exchange distance 2*half: 16, 8, 4, 2
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+            const T send = hi ? v[j] : v[j + half];
+            const T keep = hi ? v[j + half] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 2 * half);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+constexpr int kBackThreads = 128;
+
+// grad_pose: [nframes][12] doubles (dL/dR row-major, dL/dt), accumulated.
+// grad_depth: [nframes][H][W] of T, accumulated.
+// One thread per voxel, one CTA per kBackThreads voxels (CTAs finish
+// independently, so warps with little work do not hold up the others).  The
+// chunk's per-frame (D, W) history sits in shared memory, so the frame loops
+// need no unrolling.  Pose sums: per warp and frame the 12 values are reduced
+// across the warp in T, added into the CTA's shared accumulators in T, and
+// each CTA adds its non-zero totals into grad_pose in double.
+template <typename T>
+__global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, const T* gD_in, const T* gW_in,
+                                                                const T* D0, const T* W0, const T* ckpt,
+                                                                const T* depth, const T* rot, const T* trans,
+                                                                T* grad_depth, double* grad_pose, T* gD0, T* gW0) {
+    __shared__ T s_pose[kBatchMaxFrames][12];
+    __shared__ T s_acc[kBatchMaxFrames][12];
+    __shared__ T s_hist[2 * kChunk][kBackThreads];   // D then W before each frame of the chunk
+    using O = Ops<T>;
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t i = blockIdx.x * (int64_t)kBackThreads + threadIdx.x;
+    const bool inside = i < n;
+    T gd = (T)0, gw = (T)0;
+    if (inside) {
+        gd = gD_in[i];
+        gw = gW_in ? gW_in[i] : (T)0;
+    }
+    const bool active = inside && (gd != (T)0 || gw != (T)0);
+    if (!__syncthreads_or(active)) {
+        if (inside && gD0) gD0[i] = gd;
+        if (inside && gW0) gW0[i] = gw;
+        return;
+    }
+    load_poses<T>(g, rot, trans, s_pose);
+    for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) s_acc[e / 12][e % 12] = (T)0;
+    __syncthreads();
+    const int64_t frame = (int64_t)g.width * g.height;
+    const T M = (T)g.max_weight;
+    const T tr = (T)g.trunc;
+    const T half_inv = O::div((T)2, tr);
+    const int lane = threadIdx.x & 31;
+    const int t = threadIdx.x;
+    T px = 0, py = 0, pz = 0;
+    if (inside) voxel_xyz<T>(g, i, &px, &py, &pz);
+    const bool warp_active = __any_sync(0xffffffffu, active);
+    const int nchunks = (g.nframes + kChunk - 1) / kChunk;
+    for (int c = nchunks - 1; c >= 0 && warp_active; --c) {
+        const int f0 = c * kChunk;
+        const int nk = min(kChunk, g.nframes - f0);
+        // recompute the chunk forward from its starting state
+        T d = (T)0, w = (T)0;
+        unsigned seen = 0;   // bit k: frame f0 + k gave this voxel a sample
+        if (active) {
+            if (c == 0) {
+                d = D0[i];
+                w = W0[i];
+            } else {
+                const T* cp = ckpt + (int64_t)(c - 1) * 2 * n;
+                d = cp[i];
+                w = cp[n + i];
+            }
+        }
+#pragma unroll 1
+        for (int k = 0; k < nk; ++k) {
+            s_hist[k][t] = d;
+            s_hist[kChunk + k][t] = w;
             if (active) {
                 Sample<T> s;
-                sample<T>(g, R, R + 9, depth + f * frame, px, py, pz, s);
-                if (s.valid) {
-                    ++m;
-                    if (!s.truncated) {
-                        const T gs = O::mul(gD, beta<T>(m, nupd, w0, (T)g.max_weight));   // dL/dsdf
-                        // bilinear weights -> depth gradient
-                        T* gd = grad_depth + f * frame + (int64_t)s.v0 * g.width + s.u0;
-                        const T ia = O::sub((T)1, s.a), ib = O::sub((T)1, s.b);
-                        atomicAdd(gd, O::mul(gs, O::mul(ia, ib)));
-                        atomicAdd(gd + 1, O::mul(gs, O::mul(s.a, ib)));
-                        atomicAdd(gd + g.width, O::mul(gs, O::mul(ia, s.b)));
-                        atomicAdd(gd + g.width + 1, O::mul(gs, O::mul(s.a, s.b)));
-                        // d sdf / d(u, v), then through the projection
-                        const T top = O::fma(s.a, O::sub(s.d10, s.d00), s.d00);
-                        const T bot = O::fma(s.a, O::sub(s.d11, s.d01), s.d01);
-                        const T ddu = O::fma(s.b, O::sub(O::sub(s.d11, s.d01), O::sub(s.d10, s.d00)),
-                                             O::sub(s.d10, s.d00));
-                        const T ddv = O::sub(bot, top);
-                        const T gu = O::mul(gs, O::mul(ddu, (T)g.fx));
-                        const T gv = O::mul(gs, O::mul(ddv, (T)g.fy));
-                        // u = fx cx/cz + .. -> du/dcx = fx/cz, du/dcz = -fx cx/cz^2
-                        const T gcx = O::mul(gu, s.rz);
-                        const T gcy = O::mul(gv, s.rz);
-                        const T gcz = O::sub(O::mul((T)-1, gs),
-                                             O::mul(s.rz, O::add(O::mul(gcx, s.cx), O::mul(gcy, s.cy))));
-                        acc[0] = O::mul(gcx, px); acc[1] = O::mul(gcx, py); acc[2] = O::mul(gcx, pz);
-                        acc[3] = O::mul(gcy, px); acc[4] = O::mul(gcy, py); acc[5] = O::mul(gcy, pz);
-                        acc[6] = O::mul(gcz, px); acc[7] = O::mul(gcz, py); acc[8] = O::mul(gcz, pz);
-                        acc[9] = gcx; acc[10] = gcy; acc[11] = gcz;
-                        any = true;
-                    }
-                }
-            }
-            if (__any_sync(0xffffffffu, any)) {
-#pragma unroll
-                for (int k = 0; k < 12; ++k) {
-                    double v = (double)acc[k];
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    if (lane == 0 && v != 0.0) atomicAdd(&s_acc[f][k], v);
+                sample<T>(g, s_pose[f0 + k], s_pose[f0 + k] + 9, depth + (f0 + k) * frame, px, py, pz, s);
+                if (s.w > (T)0) {
+                    update<T>(d, w, s, M);
+                    seen |= 1u << k;
                 }
             }
         }
+        // reverse through the chunk
+#pragma unroll 1
+        for (int k = nk - 1; k >= 0; --k) {
+            const int f = f0 + k;
+            const bool here = (seen >> k) & 1u;
+            if (!__any_sync(0xffffffffu, here)) continue;
+            T acc[12];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) acc[q] = (T)0;
+            if (here) {
+                Sample<T> s;
+                sample<T>(g, s_pose[f], s_pose[f] + 9, depth + f * frame, px, py, pz, s);
+                const T dprev = s_hist[k][t], wprev = s_hist[kChunk + k][t];
+                const T sw = O::add(wprev, s.w);
+                const T isw = O::rcp(sw);
+                const T diff = O::sub(s.tsdf, dprev);
+                const bool sat = !(sw < M);
+                const T isw2 = O::mul(isw, isw);
+                const T g_t = O::mul(gd, O::mul(s.w, isw));
+                const T g_w = O::add(O::mul(gd, O::mul(O::mul(diff, wprev), isw2)), sat ? (T)0 : gw);
+                const T gw_prev = O::add(O::mul(gd, O::mul(O::mul(-s.w, diff), isw2)), sat ? (T)0 : gw);
+                gd = O::mul(gd, O::mul(wprev, isw));
+                gw = gw_prev;
+                // through tsdf = min(sdf, trunc), the ramp and wv
+                T g_sdf = s.truncated ? (T)0 : g_t;
+                if (s.band == 1) g_sdf = O::add(g_sdf, O::mul(g_w, O::mul(s.wv, half_inv)));
+                const T g_wv = O::mul(g_w, s.wband);
+                // d = N / wv over the valid pixels; sdf = d - z
+                const T ia = O::sub((T)1, s.a), ib = O::sub((T)1, s.b);
+                const T bw[4] = {O::mul(ia, ib), O::mul(s.a, ib), O::mul(ia, s.b), O::mul(s.a, s.b)};
+                const T dba[4] = {-ib, ib, -s.b, s.b};   // d b_i / d a
+                const T dbb[4] = {-ia, -s.a, ia, s.a};   // d b_i / d b
+                const T iwv = O::rcp(s.wv);
+                const T g_sdf_n = O::mul(g_sdf, iwv);
+                T g_a = (T)0, g_b = (T)0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (!(s.vmask & (1 << q))) continue;
+                    const T gdq = O::mul(g_sdf_n, bw[q]);
+                    if (gdq != (T)0) {
+                        const int x = s.u0 + (q & 1), y = s.v0 + (q >> 1);
+                        atomicAdd(grad_depth + f * frame + (int64_t)y * g.width + x, gdq);
+                    }
+                    // d(N / wv)/da = sum_i dba_i (d_i - d) / wv; d wv / da = sum_i dba_i
+                    const T e = O::fma(g_sdf_n, O::sub(s.d[q], s.dn), g_wv);
+                    g_a = O::fma(dba[q], e, g_a);
+                    g_b = O::fma(dbb[q], e, g_b);
+                }
+                const T gcx = O::mul(O::mul(g_a, (T)g.fx), s.rz);
+                const T gcy = O::mul(O::mul(g_b, (T)g.fy), s.rz);
+                const T gcz = O::sub(-g_sdf, O::mul(s.rz, O::fma(gcx, s.cx, O::mul(gcy, s.cy))));
+                acc[0] = O::mul(gcx, px); acc[1] = O::mul(gcx, py); acc[2] = O::mul(gcx, pz);
+                acc[3] = O::mul(gcy, px); acc[4] = O::mul(gcy, py); acc[5] = O::mul(gcy, pz);
+                acc[6] = O::mul(gcz, px); acc[7] = O::mul(gcz, py); acc[8] = O::mul(gcz, pz);
+                acc[9] = gcx; acc[10] = gcy; acc[11] = gcz;
+            }
+            const T tot = warp_sum12<T>(acc, lane);
+            if (!(lane & 1) && lane < 24 && tot != (T)0) atomicAdd(&s_acc[f][lane >> 1], tot);
+        }
     }
+    if (inside && gD0) gD0[i] = gd;
+    if (inside && gW0) gW0[i] = gw;
     __syncthreads();
-    for (int e = threadIdx.x; e < g.nframes * 12; e += blockDim.x) {
-        const double v = s_acc[e / 12][e % 12];
+    for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) {
+        const double v = (double)s_acc[e / 12][e % 12];
         if (v != 0.0) atomicAdd(grad_pose + e, v);
     }
 }
 
-template <typename T> Geometry geometry(const DiffArgs& a) {
+Geometry geometry(const DiffArgs& a) {
     Geometry g;
     g.nx = a.nx;
     g.ny = a.ny;
@@ -328,33 +416,35 @@ int grid_for(int64_t n) {
     return (int)(g < cap ? (g < 1 ? 1 : g) : cap);
 }
 
+unsigned back_grid(int64_t n) { return (unsigned)((n + kBackThreads - 1) / kBackThreads); }
+
 }  // namespace diff
 
 cudaError_t launch_diff_forward(const DiffArgs& a, cudaStream_t s) {
     const int64_t n = (int64_t)a.nx * a.ny * a.nz;
-    if (a.dtype == 1) {
+    if (a.dtype == 1)
         diff::forward_kernel<double><<<diff::grid_for(n), 256, 0, s>>>(
-            diff::geometry<double>(a), (double*)a.D, (double*)a.W, a.count, a.signature, (const double*)a.depth,
+            diff::geometry(a), (double*)a.D, (double*)a.W, (double*)a.ckpt, a.signature, (const double*)a.depth,
             (const double*)a.rot, (const double*)a.trans);
-    } else {
+    else
         diff::forward_kernel<float><<<diff::grid_for(n), 256, 0, s>>>(
-            diff::geometry<float>(a), (float*)a.D, (float*)a.W, a.count, a.signature, (const float*)a.depth,
+            diff::geometry(a), (float*)a.D, (float*)a.W, (float*)a.ckpt, a.signature, (const float*)a.depth,
             (const float*)a.rot, (const float*)a.trans);
-    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_diff_backward(const DiffArgs& a, cudaStream_t s) {
     const int64_t n = (int64_t)a.nx * a.ny * a.nz;
-    if (a.dtype == 1) {
-        diff::backward_kernel<double><<<diff::grid_for(n), 256, 0, s>>>(
-            diff::geometry<double>(a), (const double*)a.grad_D, (const double*)a.W, a.count, (const double*)a.depth,
-            (const double*)a.rot, (const double*)a.trans, (double*)a.grad_depth, a.grad_pose, (double*)a.grad_D0);
-    } else {
-        diff::backward_kernel<float><<<diff::grid_for(n), 256, 0, s>>>(
-            diff::geometry<float>(a), (const float*)a.grad_D, (const float*)a.W, a.count, (const float*)a.depth,
-            (const float*)a.rot, (const float*)a.trans, (float*)a.grad_depth, a.grad_pose, (float*)a.grad_D0);
-    }
+    if (a.dtype == 1)
+        diff::backward_kernel<double><<<diff::back_grid(n), diff::kBackThreads, 0, s>>>(
+            diff::geometry(a), (const double*)a.grad_D, (const double*)a.grad_W, (const double*)a.D,
+            (const double*)a.W, (const double*)a.ckpt, (const double*)a.depth, (const double*)a.rot,
+            (const double*)a.trans, (double*)a.grad_depth, a.grad_pose, (double*)a.grad_D0, (double*)a.grad_W0);
+    else
+        diff::backward_kernel<float><<<diff::back_grid(n), diff::kBackThreads, 0, s>>>(
+            diff::geometry(a), (const float*)a.grad_D, (const float*)a.grad_W, (const float*)a.D, (const float*)a.W,
+            (const float*)a.ckpt, (const float*)a.depth, (const float*)a.rot, (const float*)a.trans, (float*)a.grad_depth,
+            a.grad_pose, (float*)a.grad_D0, (float*)a.grad_W0);
     return cudaGetLastError();
 }
 

@@ -90,6 +90,7 @@ class BatchItem(C.Structure):
 
 
 MAX_FRAMES_PER_SCENE_PASS = 128
+DIFF_CHUNK_FRAMES = 8
 
 # (name, restype, argtypes) of every exported entry point, in header order.
 SIGNATURES = [
@@ -104,10 +105,11 @@ SIGNATURES = [
     ("gbt_batch_destroy", C.c_int, [C.c_void_p]),
     ("gbt_integrate_batch", C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int32, C.POINTER(Frame), C.c_int32,
                                       C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
-    ("gbt_diff_forward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
-                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    ("gbt_diff_backward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
-                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("gbt_diff_forward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("gbt_diff_backward", C.c_int, [C.POINTER(DiffCfg), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     ("gbt_extract_mesh", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                    C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,

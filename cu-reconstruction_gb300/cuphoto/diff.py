@@ -4,10 +4,12 @@
 
 depth [F, H, W] metres, R [F, 3, 3] world-to-camera rotations, t [F, 3]
 (float32 or float64 CUDA tensors of one dtype); D0, W0 the starting
-distances and weights [nz, ny, nx].  Gradients flow to depth, R, t and D0
-(W is piecewise constant).  The adjoint is the engine's gbt_diff_backward:
-one recomputation of each voxel-frame, no per-frame volumes kept.  Sequences
-longer than 128 frames are integrated in chunks, chained through D.
+distances and weights [nz, ny, nx].  Gradients flow to depth, R, t, D0 and
+W0 from both outputs.  The adjoint is the engine's gbt_diff_backward: reverse
+mode through the weighted running mean, recomputing each chunk of
+GBT_DIFF_CHUNK_FRAMES frames from the (D, W) checkpoints the forward wrote,
+so no per-frame volumes are kept.  Sequences longer than 128 frames are
+integrated in calls of 128 frames chained through (D, W).
 """
 import ctypes as C
 from dataclasses import dataclass
@@ -16,6 +18,7 @@ from . import _lib as L
 from .tsdf import _stream_handle
 
 MAX_FRAMES = L.MAX_FRAMES_PER_SCENE_PASS
+CHUNK = L.DIFF_CHUNK_FRAMES
 
 
 @dataclass
@@ -58,19 +61,33 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def forward_raw(cfg, D, W, depth, R, t, counts, signature=None, stream=None):
-    """In place on D, W; fills counts (int16 storage of the uint16 counts)."""
-    c = cfg.to_c(depth.shape[2], depth.shape[1], depth.dtype)
-    L.check(L.lib().gbt_diff_forward(C.byref(c), _ptr(D), _ptr(W), _ptr(counts), _ptr(depth), int(depth.shape[0]),
-                                     _ptr(R), _ptr(t), _ptr(signature) if signature is not None else None,
-                                     _stream_handle(stream)))
+def _opt(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
 
 
-def backward_raw(cfg, grad_D, W0, counts, depth, R, t, grad_depth, grad_pose, grad_D0=None, stream=None):
+def checkpoint_shape(nframes, grid_zyx):
+    """Shape of the forward's checkpoint buffer: (D, W) before every chunk of
+    CHUNK frames after the first."""
+    return (max(-(-int(nframes) // CHUNK) - 1, 0), 2) + tuple(int(x) for x in grid_zyx)
+
+
+def forward_raw(cfg, D, W, depth, R, t, checkpoints=None, signature=None, stream=None):
+    """In place on D, W.  checkpoints (checkpoint_shape, D's dtype) is needed
+    by the adjoint when there are more than CHUNK frames; signature (int32,
+    D's shape) receives the per-voxel decision hash."""
     c = cfg.to_c(depth.shape[2], depth.shape[1], depth.dtype)
-    L.check(L.lib().gbt_diff_backward(C.byref(c), _ptr(grad_D), _ptr(W0), _ptr(counts), _ptr(depth),
-                                      int(depth.shape[0]), _ptr(R), _ptr(t), _ptr(grad_depth), _ptr(grad_pose),
-                                      _ptr(grad_D0) if grad_D0 is not None else None, _stream_handle(stream)))
+    L.check(L.lib().gbt_diff_forward(C.byref(c), _ptr(D), _ptr(W), _opt(checkpoints), _opt(signature), _ptr(depth),
+                                     int(depth.shape[0]), _ptr(R), _ptr(t), _stream_handle(stream)))
+
+
+def backward_raw(cfg, grad_D, grad_W, D0, W0, checkpoints, depth, R, t, grad_depth, grad_pose, grad_D0=None,
+                 grad_W0=None, stream=None):
+    """Adds dL/ddepth into grad_depth (depth's dtype and shape) and dL/dR, dL/dt
+    into grad_pose (float64 [F, 12]); writes dL/dD0, dL/dW0 when given."""
+    c = cfg.to_c(depth.shape[2], depth.shape[1], depth.dtype)
+    L.check(L.lib().gbt_diff_backward(C.byref(c), _ptr(grad_D), _opt(grad_W), _ptr(D0), _ptr(W0), _opt(checkpoints),
+                                      _ptr(depth), int(depth.shape[0]), _ptr(R), _ptr(t), _ptr(grad_depth),
+                                      _ptr(grad_pose), _opt(grad_D0), _opt(grad_W0), _stream_handle(stream)))
 
 
 def _function():
@@ -80,32 +97,35 @@ def _function():
         @staticmethod
         def forward(ctx, depth, R, t, D0, W0, cfg):
             depth, R, t = depth.contiguous(), R.contiguous(), t.contiguous()
+            D0, W0 = D0.detach().contiguous(), W0.detach().contiguous()
             if not (depth.dtype == R.dtype == t.dtype == D0.dtype == W0.dtype):
                 raise TypeError("depth, R, t, D0 and W0 need one dtype")
             if depth.shape[0] > MAX_FRAMES:
                 raise ValueError("at most %d frames per call" % MAX_FRAMES)
-            D = D0.detach().clone()
-            W = W0.detach().clone()
-            counts = torch.empty(D.shape, dtype=torch.int16, device=D.device)
-            forward_raw(cfg, D, W, depth, R, t, counts)
-            ctx.save_for_backward(depth, R, t, W0.detach(), counts)
+            D = D0.clone()
+            W = W0.clone()
+            ckpt = torch.empty(checkpoint_shape(depth.shape[0], D.shape), dtype=D.dtype, device=D.device)
+            forward_raw(cfg, D, W, depth, R, t, ckpt if ckpt.numel() else None)
+            ctx.save_for_backward(depth, R, t, D0, W0, ckpt)
             ctx.cfg = cfg
-            ctx.mark_non_differentiable(W)
             return D, W
 
         @staticmethod
         def backward(ctx, gD, gW):
-            depth, R, t, W0, counts = ctx.saved_tensors
+            depth, R, t, D0, W0, ckpt = ctx.saved_tensors
+            need = ctx.needs_input_grad
             gdep = torch.zeros_like(depth)
             gpose = torch.zeros((depth.shape[0], 12), dtype=torch.float64, device=depth.device)
-            gD0 = torch.empty_like(W0) if ctx.needs_input_grad[3] else None
-            if gD is None:
-                gD = torch.zeros_like(W0)
-            backward_raw(ctx.cfg, gD.contiguous(), W0, counts, depth, R, t, gdep, gpose, gD0)
+            gD0 = torch.empty_like(D0) if need[3] else None
+            gW0 = torch.empty_like(W0) if need[4] else None
+            gD = torch.zeros_like(D0) if gD is None else gD.contiguous().to(D0.dtype)
+            gW = None if gW is None else gW.contiguous().to(W0.dtype)
+            backward_raw(ctx.cfg, gD, gW, D0, W0, ckpt if ckpt.numel() else None, depth, R, t, gdep, gpose, gD0,
+                         gW0)
             gR = gpose[:, :9].reshape(-1, 3, 3).to(R.dtype)
             gt = gpose[:, 9:].to(t.dtype)
-            return (gdep if ctx.needs_input_grad[0] else None, gR if ctx.needs_input_grad[1] else None,
-                    gt if ctx.needs_input_grad[2] else None, gD0, None, None)
+            return (gdep if need[0] else None, gR if need[1] else None, gt if need[2] else None,
+                    gD0, gW0, None)
 
     return IntegrateFn
 
@@ -114,7 +134,7 @@ _FN = None
 
 
 def integrate(depth, R, t, D0, W0, cfg):
-    """Differentiable integrate of F frames (chunks of 128 chained through D)."""
+    """Differentiable integrate of F frames (calls of 128 frames chained through D, W)."""
     global _FN
     if _FN is None:
         _FN = _function()
@@ -125,10 +145,52 @@ def integrate(depth, R, t, D0, W0, cfg):
 
 
 def se3_gradient(grad_R, grad_t, R, t):
-    """dL/d(rho, phi) per frame for the left perturbation exp(xi^) T from
-    dL/dR, dL/dt: rho = dL/dt, phi = vee(G R^T - R G^T)/... written out."""
+    """dL/dxi per frame, xi = (rho, phi), for the left update
+    R <- exp(phi^) R, t <- exp(phi^) t + rho, from dL/dR and dL/dt:
+    dL/drho = dL/dt, dL/dphi = vee(G R^T - R G^T) + t x dL/dt."""
     import torch
     A = grad_R @ R.transpose(1, 2)
     phi = torch.stack([A[:, 2, 1] - A[:, 1, 2], A[:, 0, 2] - A[:, 2, 0], A[:, 1, 0] - A[:, 0, 1]], -1)
     phi = phi + torch.linalg.cross(t, grad_t, dim=-1)
     return torch.cat([grad_t, phi], -1)
+
+
+def so3_exp(phi):
+    """Rotation matrices [F, 3, 3] of axis-angle vectors phi [F, 3] (Rodrigues)."""
+    import torch
+    th = phi.norm(dim=-1, keepdim=True).unsqueeze(-1)
+    K = torch.zeros(phi.shape[0], 3, 3, dtype=phi.dtype, device=phi.device)
+    K[:, 0, 1], K[:, 0, 2], K[:, 1, 2] = -phi[:, 2], phi[:, 1], -phi[:, 0]
+    K[:, 1, 0], K[:, 2, 0], K[:, 2, 1] = phi[:, 2], -phi[:, 1], phi[:, 0]
+    small = th < 1e-12
+    ths = torch.where(small, torch.ones_like(th), th)
+    a = torch.where(small, torch.ones_like(th), torch.sin(ths) / ths)
+    b = torch.where(small, 0.5 * torch.ones_like(th), (1 - torch.cos(ths)) / ths ** 2)
+    eye = torch.eye(3, dtype=phi.dtype, device=phi.device).expand_as(K)
+    return eye + a * K + b * (K @ K)
+
+
+def se3_left_update(R, t, xi):
+    """R <- exp(phi^) R, t <- exp(phi^) t + rho for xi = (rho, phi) [F, 6];
+    the camera centre -R^T t stays put when rho = 0."""
+    dR = so3_exp(xi[:, 3:].to(R.dtype))
+    return dR @ R, (dR @ t.unsqueeze(-1)).squeeze(-1) + xi[:, :3].to(t.dtype)
+
+
+def surface_alignment_error(depth, R, t, R_true, t_true, fx, fy, cx, cy):
+    """Per frame, the RMS distance (metres) between each valid depth pixel's
+    world point under (R, t) and under (R_true, t_true): the registration
+    error of the frame's surface, which weighs rotation by scene depth."""
+    import torch
+    H, W = depth.shape[1:]
+    v, u = torch.meshgrid(torch.arange(H, device=depth.device, dtype=torch.float64),
+                          torch.arange(W, device=depth.device, dtype=torch.float64), indexing="ij")
+    out = []
+    for k in range(depth.shape[0]):
+        z = depth[k].double()
+        m = z > 0
+        pc = torch.stack([(u[m] - cx) / fx * z[m], (v[m] - cy) / fy * z[m], z[m]], -1)
+        pe = (pc - t[k].double()) @ R[k].double()
+        pt = (pc - t_true[k].double()) @ R_true[k].double()
+        out.append(((pe - pt) ** 2).sum(-1).mean().sqrt())
+    return torch.stack(out)

@@ -232,6 +232,71 @@ def frontal_poses(n, seed=0, jitter_deg=2.0, jitter_m=0.05):
     return np.array(out)
 
 
+def axis_angle_matrix(w):
+    """Rotation matrix of the axis-angle vector w (Rodrigues)."""
+    w = np.asarray(w, np.float64)
+    th = np.linalg.norm(w)
+    K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    if th < 1e-12:
+        return np.eye(3) + K
+    return np.eye(3) + np.sin(th) / th * K + (1 - np.cos(th)) / th ** 2 * K @ K
+
+
+def jitter_poses(R, t, frames, deg, metres, seed):
+    """Left-perturb the listed frames of world-to-camera (R [F,3,3], t [F,3]):
+    a rotation of `deg` about a random axis through the camera centre, then a
+    translation of `metres` in a random direction."""
+    rng = np.random.default_rng(seed)
+    R, t = np.array(R, np.float64), np.array(t, np.float64)
+    for k in frames:
+        ax = rng.normal(size=3)
+        dR = axis_angle_matrix(np.deg2rad(deg) * ax / np.linalg.norm(ax))
+        d = rng.normal(size=3)
+        R[k] = dR @ R[k]
+        t[k] = dR @ t[k] + metres * d / np.linalg.norm(d)
+    return R, t
+
+
+def diff_case_frontal(n=128, frames=16, camera=None, scene_id=5):
+    """The differentiable-integrate check configuration: the frontal scene
+    seen from `frames` poses jittered by up to 3 deg / 5 cm, float64 depth
+    metres without noise, an n^3 grid over 2.0 x 1.6 x 2.4 m starting 0.4 m in
+    front of the first camera, truncation 4 voxels, and the analytic
+    truncated SDF of the scene as the loss target.  Returns a dict of arrays
+    (R [F,3,3], t [F,3], depth [F,H,W], gt [nz,ny,nx]) and the cfg fields."""
+    cam = camera or Camera.half()
+    scene = make_frontal_scene(scene_id)
+    poses = frontal_poses(frames, seed=scene_id, jitter_deg=3.0, jitter_m=0.05)
+    depth = np.stack([render_depth_m(scene, p, cam) for p in poses])
+    depth = np.where(np.isfinite(depth) & (depth < 8.0), depth, 0.0)
+    grid = (n, n, n)
+    vs = (np.array([2.0, 1.6, 2.4]) / n).astype(np.float32)
+    off = np.array([-1.0, -0.8, 0.4], np.float32)
+    trunc = float(np.float32(4 * vs.max()))
+    R = np.stack([matrix_from_quat(p[:4]) for p in poses])
+    t = np.stack([p[4:] for p in poses])
+    return dict(grid=grid, vs=vs, off=off, K=(cam.fx, cam.fy, cam.cx, cam.cy), trunc=trunc, max_weight=128.0,
+                max_depth=8.0, min_z=0.05, width=cam.width, height=cam.height, depth=depth, R=R, t=t,
+                gt=sdf_gt(scene, grid, vs, off, trunc))
+
+
+def diff_case_circle(n=128, frames=16, camera=None, scene_id=5, n_spheres=12):
+    """The pose-refinement setting: spheres on a ground plane seen from a
+    circle of cameras, float64 depth metres without noise, an n^3 grid over
+    the 2.56 m cube, truncation 4 voxels."""
+    cam = camera or Camera(320, 240, 262.5, 262.5, 159.5, 119.5)
+    scene = make_scene(scene_id, n_spheres=n_spheres)
+    poses = circle_poses(frames)
+    depth = np.stack([render_depth_m(scene, p, cam) for p in poses])
+    depth = np.where(np.isfinite(depth) & (depth < 8.0), depth, 0.0)
+    vs = np.full(3, 2.56 / n, np.float32)
+    R = np.stack([matrix_from_quat(p[:4]) for p in poses])
+    t = np.stack([p[4:] for p in poses])
+    return dict(grid=(n, n, n), vs=vs, off=np.full(3, -1.28, np.float32), K=(cam.fx, cam.fy, cam.cx, cam.cy),
+                trunc=float(np.float32(4 * vs[0])), max_weight=128.0, max_depth=8.0, min_z=0.05, width=cam.width,
+                height=cam.height, depth=depth, R=R, t=t, scene=scene)
+
+
 def make_sequence(n_frames, scene_id=0, camera=None, n_spheres=6, trajectory="circle", **kw):
     camera = camera or Camera()
     if trajectory == "frontal":

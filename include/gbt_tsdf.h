@@ -179,48 +179,63 @@ gbt_status gbt_integrate_batch(gbt_batch* batch, const gbt_batch_item* items, in
                                void* stream);
 
 /* Differentiable integrate.  No counterpart in the reference (its integrate
- * is not differentiable); it follows the fixed mode with bilinear depth
- * sampling so the volume is differentiable in each depth pixel and in each
- * frame's pose:  c = R p + t, (u, v) = (fx c.x/z + cx, fy c.y/z + cy),
- * d = bilinear(depth, u, v) over four valid pixels, sdf = d - z,
- * tsdf = min(sdf, truncation), D += (tsdf - D)/(w + 1), w = min(w + 1, max_weight),
- * for z > min_z, the 2x2 footprint inside the image, sdf >= -truncation.
+ * is not differentiable).  It follows the fixed mode with bilinear depth
+ * sampling and continuous sample weights, so the volume is differentiable in
+ * each depth pixel and in each frame's pose:
+ *   c = R p + t, (u, v) = (fx c.x/z + cx, fy c.y/z + cy),
+ *   the 2x2 pixel footprint around (u, v), bilinear weights b_i, validity
+ *     v_i = 1 for a pixel inside the image with depth in (0, max_depth],
+ *   wv = sum b_i v_i, d = sum b_i v_i depth_i / wv, sdf = d - z,
+ *   tsdf = min(sdf, truncation), w = wv * ramp((sdf + tr)/(tr/2)),
+ *     ramp = clamp(., 0, 1), tr = truncation,
+ *   D += w (tsdf - D)/(W + w), W = min(W + w, max_weight)    (for w > 0)
+ * for z > min_z and u, v in (-1, width), (-1, height).  The sample weight
+ * falls to zero continuously as the footprint leaves the image or the valid
+ * depth and at the back of the truncation band, which keeps D and W
+ * continuous (z = min_z is the one hard cut).
  *
  * Tensors are caller-owned device arrays of `dtype` (0 float32, 1 float64):
  * tsdf/weights [nz][ny][nx], depth [nframes][height][width] metres,
  * rot [nframes][9] (row-major world-to-camera rotation), trans [nframes][3].
  * nframes <= GBT_MAX_FRAMES_PER_SCENE_PASS per call. */
+#define GBT_DIFF_CHUNK_FRAMES 8
 typedef struct {
     uint32_t voxel_grid_size[3];
     float voxel_size[3];
     float global_offset[3];
     float focal_x, focal_y, cx, cy;
     float truncation;        /* > 0 */
-    float max_weight;        /* >= 1 */
+    float max_weight;        /* > 0 */
     float max_depth;         /* > 0 */
     float min_z;
     int32_t width, height;   /* depth image size */
     int32_t dtype;           /* 0 float32, 1 float64 */
 } gbt_diff_cfg;
 
-/* Forward: updates tsdf/weights in place and writes counts[v], the number of
- * updates voxel v received.  signature (optional, NULL) receives a per-voxel
- * hash of the discrete decisions (validity, truncation, pixel cell): voxels
- * whose hash changes between two poses are not smooth between them. */
-gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, uint16_t* counts, const void* depth,
-                            int32_t nframes, const void* rot, const void* trans, uint32_t* signature, void* stream);
+/* Forward: updates tsdf/weights in place.  checkpoints (needed by the
+ * adjoint, else NULL) receives (tsdf, weights) before every chunk of
+ * GBT_DIFF_CHUNK_FRAMES frames after the first: (ceil(nframes/8) - 1) x 2 x
+ * nvoxels values of dtype.  signature (optional) receives a per-voxel hash of
+ * the discrete decisions (footprint cell, ramp and clamp states): voxels
+ * whose hash changes between two inputs are not smooth between them. */
+gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, void* checkpoints,
+                            uint32_t* signature, const void* depth, int32_t nframes, const void* rot,
+                            const void* trans, void* stream);
 
-/* Adjoint of gbt_diff_forward for a gradient dL/dtsdf of the final distances:
- * adds dL/ddepth into grad_depth ([nframes][height][width], dtype) and
- * dL/dR, dL/dt into grad_pose ([nframes][12] float64: 9 row-major, then 3),
- * and writes dL/dtsdf of the distances before the forward into
- * grad_tsdf_before when it is not NULL (for chaining calls).
- * weights_before are the weights the forward started from; counts are the
- * forward's.  Recomputes each voxel-frame once; stores nothing per frame. */
-gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* weights_before,
-                             const uint16_t* counts, const void* depth, int32_t nframes, const void* rot,
-                             const void* trans, void* grad_depth, double* grad_pose, void* grad_tsdf_before,
-                             void* stream);
+/* Adjoint of gbt_diff_forward (reverse mode, frame-chunk recomputation from
+ * the checkpoints; no per-frame volumes).  Inputs: dL/dtsdf and, optionally,
+ * dL/dweights of the final volume, the volume before the forward and the
+ * forward's checkpoints.  Adds dL/ddepth into grad_depth ([nframes][height]
+ * [width] of dtype) and dL/dR, dL/dt into grad_pose ([nframes][12] float64:
+ * 9 row-major, then 3); writes dL/dtsdf and dL/dweights of the volume before
+ * the forward when those pointers are not NULL (for chaining calls).  In
+ * float32 the per-frame pose sums are formed in float32 per CTA and added
+ * across CTAs in float64. */
+gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, const void* grad_weights,
+                             const void* tsdf_before, const void* weights_before, const void* checkpoints,
+                             const void* depth, int32_t nframes, const void* rot, const void* trans,
+                             void* grad_depth, double* grad_pose, void* grad_tsdf_before,
+                             void* grad_weights_before, void* stream);
 
 /* Replaces generate_triangular_surface (marching_cubes.cu:191-237).
  * Writes up to cap_tris triangles: verts gets 9 floats per triangle (three

@@ -168,35 +168,37 @@ def _diff_lib():
     so = lib()
     if not getattr(so, "_diff_ready", False):
         vp = C.c_void_p
-        so.oracle_diff_forward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, vp, vp, C.c_int32, vp, vp, C.c_int32]
-        so.oracle_diff_backward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, C.c_int32, vp, vp, vp, vp]
+        so.oracle_diff_forward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, vp, C.c_int32, vp, vp, C.c_int32]
+        so.oracle_diff_backward.argtypes = [C.POINTER(OracleDiffCfg), vp, vp, vp, vp, vp, C.c_int32, vp, vp, vp, vp,
+                                            vp, vp]
         so._diff_ready = True
     return so
 
 
 def diff_forward(cfg, D, W, depth, rot, trans, threads=0):
-    """In place on D, W (float32 or float64 per cfg.dtype); returns (count, signature)."""
-    n = D.size
-    count = np.zeros(n, np.uint16)
-    sig = np.zeros(n, np.uint32)
+    """In place on D, W (float32 or float64 per cfg.dtype); returns the signature."""
+    sig = np.zeros(D.size, np.uint32)
     depth = np.ascontiguousarray(depth)
     rot = np.ascontiguousarray(rot)
     trans = np.ascontiguousarray(trans)
-    _diff_lib().oracle_diff_forward(C.byref(cfg), _p(D), _p(W), _p(count), _p(sig), _p(depth), len(depth), _p(rot),
-                                    _p(trans), threads)
-    return count.reshape(D.shape), sig.reshape(D.shape)
+    _diff_lib().oracle_diff_forward(C.byref(cfg), _p(D), _p(W), _p(sig), _p(depth), len(depth), _p(rot), _p(trans),
+                                    threads)
+    return sig.reshape(D.shape)
 
 
-def diff_backward(cfg, grad_D, W0, depth, rot, trans):
-    """float64 gradient: (grad_depth [F,H,W], grad_pose [F,12])."""
-    depth = np.ascontiguousarray(depth, np.float64)
+def diff_backward(cfg, grad_D, grad_W, D0, W0, depth, rot, trans):
+    """float64 reverse mode: (grad_depth [F,H,W], grad_pose [F,12], grad_D0, grad_W0)."""
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)
+    depth = f64(depth)
     gdep = np.zeros(depth.shape, np.float64)
     gpose = np.zeros((len(depth), 12), np.float64)
-    _diff_lib().oracle_diff_backward(C.byref(cfg), _p(np.ascontiguousarray(grad_D, np.float64)),
-                                     _p(np.ascontiguousarray(W0, np.float64)), _p(depth), len(depth),
-                                     _p(np.ascontiguousarray(rot, np.float64)),
-                                     _p(np.ascontiguousarray(trans, np.float64)), _p(gdep), _p(gpose))
-    return gdep, gpose
+    gD0 = np.zeros(np.shape(D0), np.float64)
+    gW0 = np.zeros(np.shape(D0), np.float64)
+    gW = None if grad_W is None else f64(grad_W)
+    _diff_lib().oracle_diff_backward(C.byref(cfg), _p(f64(grad_D)), None if gW is None else _p(gW), _p(f64(D0)),
+                                     _p(f64(W0)), _p(depth), len(depth), _p(f64(rot)), _p(f64(trans)), _p(gdep),
+                                     _p(gpose), _p(gD0), _p(gW0))
+    return gdep, gpose, gD0, gW0
 
 
 # ---------------------------------------------------------------------------

@@ -520,10 +520,11 @@ int64_t oracle_mc_fixed(const oracle_cfg* c, const float* D, const float* W, flo
 
 // ---------------------------------------------------------------------------
 // Differentiable integrate (the engine's definition, include/gbt_tsdf.h):
-// fixed-mode running average with bilinear depth sampling.  The forward is
-// restated operation for operation in float and double; the gradient is
-// computed in double by the explicit backward recurrence over each voxel's
-// list of updates (independent of the engine's closed form).
+// fixed-mode geometry, validity-normalised bilinear depth over the 2x2
+// footprint, sample weight w = (sum of the valid pixels' bilinear weights) *
+// ramp((sdf + tr)/(tr/2)), weighted running mean with clamped weight.  The forward is restated operation for operation
+// in float and double; the gradient is plain reverse mode in double over each
+// voxel's whole history (no chunks, no checkpoints).
 
 extern "C" {
 
@@ -541,70 +542,99 @@ typedef struct {
 
 namespace {
 
-template <typename T> struct DOps;
-template <> struct DOps<float> {
-    static float fma_(float a, float b, float c) { return std::fma(a, b, c); }
-    static float rcp(float a) { return 1.0f / a; }
-};
-template <> struct DOps<double> {
-    static double fma_(double a, double b, double c) { return std::fma(a, b, c); }
-    static double rcp(double a) { return 1.0 / a; }
-};
-
 template <typename T> struct DSample {
-    bool valid = false, truncated = false;
-    int u0 = 0, v0 = 0;
-    T a = 0, b = 0, d00 = 0, d10 = 0, d01 = 0, d11 = 0, cx = 0, cy = 0, cz = 0, rz = 0, sdf = 0, tsdf = 0;
+    bool truncated = false;
+    int band = 0, u0 = 0, v0 = 0, vmask = 0;
+    T a = 0, b = 0, d[4] = {0, 0, 0, 0}, wv = 0, dn = 0, cx = 0, cy = 0, cz = 0, rz = 0, sdf = 0, tsdf = 0,
+      wband = 0, w = 0;
 };
 
 template <typename T>
 T dcentre(int64_t v, float vs, float off) {
-    return DOps<T>::fma_((T)v + (T)0.5, (T)vs, (T)off);
+    return std::fma((T)v + (T)0.5, (T)vs, (T)off);
+}
+
+template <typename T>
+T dramp(T x, int* state) {
+    if (!(x > (T)0)) {
+        *state = 0;
+        return (T)0;
+    }
+    if (x >= (T)1) {
+        *state = 2;
+        return (T)1;
+    }
+    *state = 1;
+    return x;
 }
 
 template <typename T>
 DSample<T> dsample(const oracle_diff_cfg* g, const T* R, const T* t, const T* depth, T px, T py, T pz) {
-    using O = DOps<T>;
     DSample<T> s;
-    s.cz = O::fma_(R[8], pz, O::fma_(R[6], px, R[7] * py)) + t[2];
+    s.cz = std::fma(R[8], pz, std::fma(R[6], px, R[7] * py)) + t[2];
     if (!(s.cz > (T)g->min_z)) return s;
-    s.cx = O::fma_(R[2], pz, O::fma_(R[0], px, R[1] * py)) + t[0];
-    s.cy = O::fma_(R[5], pz, O::fma_(R[3], px, R[4] * py)) + t[1];
-    s.rz = O::rcp(s.cz);
-    const T u = O::fma_((T)g->fx, s.cx * s.rz, (T)g->cx);
-    const T v = O::fma_((T)g->fy, s.cy * s.rz, (T)g->cy);
-    if (!(u >= (T)0 && v >= (T)0 && u < (T)(g->width - 1) && v < (T)(g->height - 1))) return s;
+    s.cx = std::fma(R[2], pz, std::fma(R[0], px, R[1] * py)) + t[0];
+    s.cy = std::fma(R[5], pz, std::fma(R[3], px, R[4] * py)) + t[1];
+    s.rz = (T)1 / s.cz;
+    const T u = std::fma((T)g->fx, s.cx * s.rz, (T)g->cx);
+    const T v = std::fma((T)g->fy, s.cy * s.rz, (T)g->cy);
+    if (!(u > (T)-1 && v > (T)-1 && u < (T)g->width && v < (T)g->height)) return s;
     const T fu = std::floor(u), fv = std::floor(v);
     s.u0 = (int)fu;
     s.v0 = (int)fv;
     s.a = u - fu;
     s.b = v - fv;
-    const T* r0 = depth + (int64_t)s.v0 * g->width + s.u0;
-    const T* r1 = r0 + g->width;
-    s.d00 = r0[0];
-    s.d10 = r0[1];
-    s.d01 = r1[0];
-    s.d11 = r1[1];
     const T md = (T)g->max_depth;
-    if (!(s.d00 > 0 && s.d10 > 0 && s.d01 > 0 && s.d11 > 0 && s.d00 <= md && s.d10 <= md && s.d01 <= md &&
-          s.d11 <= md))
-        return s;
-    const T top = O::fma_(s.a, s.d10 - s.d00, s.d00);
-    const T bot = O::fma_(s.a, s.d11 - s.d01, s.d01);
-    const T d = O::fma_(s.b, bot - top, top);
-    s.sdf = d - s.cz;
-    if (!(s.sdf >= -(T)g->trunc)) return s;
-    s.truncated = s.sdf > (T)g->trunc;
-    s.tsdf = std::fmin(s.sdf, (T)g->trunc);
-    s.valid = true;
+    for (int k = 0; k < 4; ++k) {
+        const int x = s.u0 + (k & 1), y = s.v0 + (k >> 1);
+        T dv = 0;
+        if (x >= 0 && y >= 0 && x < g->width && y < g->height) dv = depth[(int64_t)y * g->width + x];
+        s.d[k] = dv;
+        if (dv > 0 && dv <= md) s.vmask |= 1 << k;
+    }
+    if (!s.vmask) return s;
+    const T ia = (T)1 - s.a, ib = (T)1 - s.b;
+    const T bw[4] = {ia * ib, s.a * ib, ia * s.b, s.a * s.b};
+    T wv = 0, nd = 0;
+    for (int k = 0; k < 4; ++k)
+        if (s.vmask & (1 << k)) {
+            wv = wv + bw[k];
+            nd = std::fma(bw[k], s.d[k], nd);
+        }
+    s.wv = wv;
+    if (!(wv > 0)) return s;
+    s.dn = nd / wv;
+    s.sdf = s.dn - s.cz;
+    const T tr = (T)g->trunc;
+    s.truncated = s.sdf > tr;
+    s.tsdf = std::fmin(s.sdf, tr);
+    s.wband = dramp<T>((s.sdf + tr) * ((T)2 / tr), &s.band);
+    s.w = s.wv * s.wband;
     return s;
 }
 
 template <typename T>
-void diff_forward(const oracle_diff_cfg* g, T* D, T* W, uint16_t* count, uint32_t* sig, const T* depth, int nframes,
-                  const T* rot, const T* trans, int threads) {
+uint32_t dcode(const DSample<T>& s, bool sat) {
+    if (!(s.w > (T)0)) return 0x7fffffffu;
+    return ((uint32_t)(s.u0 * 4099 + s.v0 * 7) ^ ((uint32_t)s.band << 24) ^ ((uint32_t)s.vmask << 26) ^
+            (s.truncated ? 0x80000000u : 0u) ^ (sat ? 0x40000000u : 0u));
+}
+
+template <typename T>
+bool dupdate(T& d, T& w, const DSample<T>& s, T M) {
+    const T sw = w + s.w;
+    d = std::fma(s.w, (s.tsdf - d) / sw, d);
+    const bool sat = !(sw < M);
+    w = sat ? M : sw;
+    return sat;
+}
+
+template <typename T>
+void diff_forward(const oracle_diff_cfg* g, T* D, T* W, uint32_t* sig, const T* depth, int nframes, const T* rot,
+                  const T* trans, int threads) {
     const int64_t nx = g->grid[0], ny = g->grid[1], nz = g->grid[2];
     const int64_t frame = (int64_t)g->width * g->height;
+    const T M = (T)g->max_weight;
 #pragma omp parallel for schedule(static) num_threads(nthreads(threads))
     for (int64_t i = 0; i < nx * ny * nz; ++i) {
         const int64_t x = i % nx, r = i / nx, y = r % ny, z = r / ny;
@@ -612,22 +642,15 @@ void diff_forward(const oracle_diff_cfg* g, T* D, T* W, uint16_t* count, uint32_
         const T py = dcentre<T>(y, g->vs[1], g->off[1]);
         const T pz = dcentre<T>(z, g->vs[2], g->off[2]);
         T d = D[i], w = W[i];
-        int cnt = 0;
         uint32_t h = 2166136261u;
         for (int f = 0; f < nframes; ++f) {
             const DSample<T> s = dsample<T>(g, rot + 9 * f, trans + 3 * f, depth + f * frame, px, py, pz);
-            const uint32_t code = s.valid ? (uint32_t)(s.u0 * 4099 + s.v0 * 7) ^ (s.truncated ? 0x80000000u : 0u)
-                                          : 0x7fffffffu;
-            h = (h ^ code) * 16777619u;
-            if (!s.valid) continue;
-            const T inv = DOps<T>::rcp(w + (T)1);
-            d = DOps<T>::fma_(s.tsdf - d, inv, d);
-            w = std::fmin(w + (T)1, (T)g->max_weight);
-            ++cnt;
+            bool sat = false;
+            if (s.w > (T)0) sat = dupdate<T>(d, w, s, M);
+            h = (h ^ dcode<T>(s, sat)) * 16777619u;
         }
         D[i] = d;
         W[i] = w;
-        if (count) count[i] = (uint16_t)cnt;
         if (sig) sig[i] = h;
     }
 }
@@ -636,85 +659,87 @@ void diff_forward(const oracle_diff_cfg* g, T* D, T* W, uint16_t* count, uint32_
 
 extern "C" {
 
-void oracle_diff_forward(const oracle_diff_cfg* g, void* D, void* W, uint16_t* count, uint32_t* sig, const void* depth,
+void oracle_diff_forward(const oracle_diff_cfg* g, void* D, void* W, uint32_t* sig, const void* depth,
                          int32_t nframes, const void* rot, const void* trans, int32_t threads) {
     if (g->dtype == 1)
-        diff_forward<double>(g, (double*)D, (double*)W, count, sig, (const double*)depth, nframes, (const double*)rot,
+        diff_forward<double>(g, (double*)D, (double*)W, sig, (const double*)depth, nframes, (const double*)rot,
                              (const double*)trans, threads);
     else
-        diff_forward<float>(g, (float*)D, (float*)W, count, sig, (const float*)depth, nframes, (const float*)rot,
+        diff_forward<float>(g, (float*)D, (float*)W, sig, (const float*)depth, nframes, (const float*)rot,
                             (const float*)trans, threads);
 }
 
-// Gradient in double of the final distances' loss gradient grad_D through
-// the forward that started from weights W0: grad_depth [F][H][W] and
-// grad_pose [F][12] (dL/dR row-major, dL/dt), both accumulated.
-void oracle_diff_backward(const oracle_diff_cfg* g, const double* grad_D, const double* W0, const double* depth,
-                          int32_t nframes, const double* rot, const double* trans, double* grad_depth,
-                          double* grad_pose) {
+// Reverse mode in double: gradients of a loss with dL/dD = grad_D and
+// dL/dW = grad_W (may be NULL) of the final volume, through a forward that
+// started from (D0, W0).  Accumulates grad_depth [F][H][W] and grad_pose
+// [F][12] (dL/dR row-major, dL/dt); writes grad_D0, grad_W0 when not NULL.
+void oracle_diff_backward(const oracle_diff_cfg* g, const double* grad_D, const double* grad_W, const double* D0,
+                          const double* W0, const double* depth, int32_t nframes, const double* rot,
+                          const double* trans, double* grad_depth, double* grad_pose, double* grad_D0,
+                          double* grad_W0) {
     const int64_t nx = g->grid[0], ny = g->grid[1], nz = g->grid[2];
     const int64_t frame = (int64_t)g->width * g->height;
-    const double M = g->max_weight;
-    std::vector<DSample<double>> samples;
-    std::vector<int> frames_of;
-    std::vector<double> alpha, beta;
+    const double M = g->max_weight, tr = g->trunc, half_inv = 2.0 / tr;
+    std::vector<DSample<double>> smp(nframes);
+    std::vector<double> dprev(nframes), wprev(nframes);
     for (int64_t i = 0; i < nx * ny * nz; ++i) {
-        const double gD = grad_D[i];
-        if (gD == 0.0) continue;
-        const int64_t x = i % nx, r = i / nx, y = r % ny, z = r / ny;
-        const double px = dcentre<double>(x, g->vs[0], g->off[0]);
-        const double py = dcentre<double>(y, g->vs[1], g->off[1]);
-        const double pz = dcentre<double>(z, g->vs[2], g->off[2]);
-        samples.clear();
-        frames_of.clear();
-        for (int f = 0; f < nframes; ++f) {
-            const DSample<double> s = dsample<double>(g, rot + 9 * f, trans + 3 * f, depth + f * frame, px, py, pz);
-            if (s.valid) {
-                samples.push_back(s);
-                frames_of.push_back(f);
+        double gd = grad_D[i], gw = grad_W ? grad_W[i] : 0.0;
+        if (gd != 0.0 || gw != 0.0) {
+            const int64_t x = i % nx, r = i / nx, y = r % ny, z = r / ny;
+            const double px = dcentre<double>(x, g->vs[0], g->off[0]);
+            const double py = dcentre<double>(y, g->vs[1], g->off[1]);
+            const double pz = dcentre<double>(z, g->vs[2], g->off[2]);
+            double d = D0[i], w = W0[i];
+            for (int f = 0; f < nframes; ++f) {
+                smp[f] = dsample<double>(g, rot + 9 * f, trans + 3 * f, depth + f * frame, px, py, pz);
+                dprev[f] = d;
+                wprev[f] = w;
+                if (smp[f].w > 0) dupdate<double>(d, w, smp[f], M);
+            }
+            for (int f = nframes - 1; f >= 0; --f) {
+                const DSample<double>& s = smp[f];
+                if (!(s.w > 0)) continue;
+                const double sw = wprev[f] + s.w;
+                const bool sat = !(sw < M);
+                const double diff = s.tsdf - dprev[f];
+                const double g_t = gd * s.w / sw;
+                const double g_w = gd * diff * wprev[f] / (sw * sw) + (sat ? 0.0 : gw);
+                const double gw_prev = -gd * s.w * diff / (sw * sw) + (sat ? 0.0 : gw);
+                gd = gd * wprev[f] / sw;
+                gw = gw_prev;
+                double g_sdf = s.truncated ? 0.0 : g_t;
+                if (s.band == 1) g_sdf += g_w * s.wv * half_inv;
+                const double g_wv = g_w * s.wband;
+                const double ia = 1 - s.a, ib = 1 - s.b;
+                const double bw[4] = {ia * ib, s.a * ib, ia * s.b, s.a * s.b};
+                const double dba[4] = {-ib, ib, -s.b, s.b};
+                const double dbb[4] = {-ia, -s.a, ia, s.a};
+                double g_a = 0, g_b = 0;
+                for (int q = 0; q < 4; ++q) {
+                    if (!(s.vmask & (1 << q))) continue;
+                    const int x = s.u0 + (q & 1), y = s.v0 + (q >> 1);
+                    grad_depth[f * frame + (int64_t)y * g->width + x] += g_sdf * bw[q] / s.wv;
+                    // d d / d a = sum dba (d_i - d) / wv over valid pixels; d wv / d a = sum dba
+                    g_a += dba[q] * (g_sdf * (s.d[q] - s.dn) / s.wv + g_wv);
+                    g_b += dbb[q] * (g_sdf * (s.d[q] - s.dn) / s.wv + g_wv);
+                }
+                const double gx = g_a * g->fx / s.cz;
+                const double gy = g_b * g->fy / s.cz;
+                const double gz = -g_sdf - (gx * s.cx + gy * s.cy) / s.cz;
+                double* gp = grad_pose + 12 * f;
+                const double p[3] = {px, py, pz};
+                for (int k = 0; k < 3; ++k) {
+                    gp[k] += gx * p[k];
+                    gp[3 + k] += gy * p[k];
+                    gp[6 + k] += gz * p[k];
+                }
+                gp[9] += gx;
+                gp[10] += gy;
+                gp[11] += gz;
             }
         }
-        const size_t n = samples.size();
-        if (!n) continue;
-        alpha.assign(n, 0.0);
-        beta.assign(n, 0.0);
-        double w = std::min(std::max(W0[i], 0.0), M);
-        for (size_t j = 0; j < n; ++j) {
-            alpha[j] = 1.0 / (w + 1.0);
-            w = std::min(w + 1.0, M);
-        }
-        double c = 1.0;
-        for (size_t j = n; j-- > 0;) {
-            beta[j] = c * alpha[j];
-            c *= 1.0 - alpha[j];
-        }
-        for (size_t j = 0; j < n; ++j) {
-            const DSample<double>& s = samples[j];
-            if (s.truncated) continue;
-            const int f = frames_of[j];
-            const double gs = gD * beta[j];
-            double* gd = grad_depth + f * frame + (int64_t)s.v0 * g->width + s.u0;
-            gd[0] += gs * (1 - s.a) * (1 - s.b);
-            gd[1] += gs * s.a * (1 - s.b);
-            gd[g->width] += gs * (1 - s.a) * s.b;
-            gd[g->width + 1] += gs * s.a * s.b;
-            const double dd_da = (1 - s.b) * (s.d10 - s.d00) + s.b * (s.d11 - s.d01);
-            const double dd_db = (1 - s.a) * (s.d01 - s.d00) + s.a * (s.d11 - s.d10);
-            // u = fx x/z + cx, v = fy y/z + cy
-            const double gx = gs * dd_da * g->fx / s.cz;
-            const double gy = gs * dd_db * g->fy / s.cz;
-            const double gz = -gs - gs * dd_da * g->fx * s.cx / (s.cz * s.cz) - gs * dd_db * g->fy * s.cy / (s.cz * s.cz);
-            double* gp = grad_pose + 12 * f;
-            const double p[3] = {px, py, pz};
-            for (int k = 0; k < 3; ++k) {
-                gp[k] += gx * p[k];
-                gp[3 + k] += gy * p[k];
-                gp[6 + k] += gz * p[k];
-            }
-            gp[9] += gx;
-            gp[10] += gy;
-            gp[11] += gz;
-        }
+        if (grad_D0) grad_D0[i] = gd;
+        if (grad_W0) grad_W0[i] = gw;
     }
 }
 

@@ -99,3 +99,67 @@ def test_null_arguments_are_rejected(engine_lib):
     assert lib.gbt_extract_mesh(None, None, None, 0, 0, C.byref(n), None) == L.GBT_ERR_INVALID_ARG
     assert lib.gbt_volume_get_info(None, None) == L.GBT_ERR_INVALID_ARG
     assert lib.gbt_volume_destroy(None) == L.GBT_OK
+
+
+def test_diff_rejects_bad_arguments(engine_lib):
+    """Argument checks of the differentiable entry points run before any
+    device work (no GPU needed)."""
+    from cuphoto import _lib as L
+    lib = L.lib()
+    c = L.DiffCfg()
+    for i in range(3):
+        c.voxel_grid_size[i] = 8
+        c.voxel_size[i] = 0.01
+    c.focal_x = c.focal_y = 50.0
+    c.truncation, c.max_weight, c.max_depth = 0.03, 8.0, 4.0
+    c.width, c.height, c.dtype = 16, 12, 0
+    p = C.c_void_p(16)
+    # NULL tensors
+    assert lib.gbt_diff_forward(C.byref(c), None, p, None, None, p, 1, p, p, None) == L.GBT_ERR_INVALID_ARG
+    # more than one chunk of frames and no checkpoints for the adjoint
+    assert lib.gbt_diff_backward(C.byref(c), p, None, p, p, None, p, 9, p, p, p, p, None, None,
+                                 None) == L.GBT_ERR_INVALID_ARG
+    assert b"checkpoints" in lib.gbt_last_error()
+    c.dtype = 2
+    assert lib.gbt_diff_forward(C.byref(c), p, p, None, None, p, 1, p, p, None) == L.GBT_ERR_INVALID_ARG
+    c.dtype = 0
+    c.truncation = 0.0
+    assert lib.gbt_diff_forward(C.byref(c), p, p, None, None, p, 1, p, p, None) == L.GBT_ERR_INVALID_ARG
+
+
+def test_se3_helpers():
+    """so3_exp against Rodrigues in numpy; se3_gradient against a central
+    difference of a smooth function of (R, t) under the left update."""
+    import numpy as np
+    import torch
+    import diffcase
+    from cuphoto.diff import checkpoint_shape, se3_gradient, se3_left_update, so3_exp
+    rng = np.random.default_rng(0)
+    phi = rng.normal(size=(5, 3))
+    phi[0] = 0
+    E = so3_exp(torch.as_tensor(phi)).numpy()
+    for k in range(5):
+        np.testing.assert_allclose(E[k], diffcase.rot_exp(phi[k]), atol=1e-14)
+    R = so3_exp(torch.as_tensor(rng.normal(size=(3, 3))))
+    t = torch.as_tensor(rng.normal(size=(3, 3)))
+    P = torch.as_tensor(rng.normal(size=(7, 3)))
+
+    def f(R, t):   # any smooth function of the world-to-camera poses
+        c = torch.einsum("fij,pj->fpi", R, P) + t[:, None, :]
+        return (torch.sin(c) * c).sum()
+
+    Rv, tv = R.clone().requires_grad_(True), t.clone().requires_grad_(True)
+    f(Rv, tv).backward()
+    g = se3_gradient(Rv.grad, tv.grad, R, t)
+    xi = torch.as_tensor(rng.normal(size=(3, 6)))
+    h = 1e-6
+    fd = (f(*se3_left_update(R, t, h * xi)) - f(*se3_left_update(R, t, -h * xi))) / (2 * h)
+    assert abs(float(fd) - float((g * xi).sum())) <= 1e-7 * abs(float(fd))
+    # the camera centre stays put under a pure rotation update
+    xi[:, :3] = 0
+    R2, t2 = se3_left_update(R, t, xi)
+    c1 = -(R.transpose(1, 2) @ t[..., None])
+    c2 = -(R2.transpose(1, 2) @ t2[..., None])
+    np.testing.assert_allclose(c1.numpy(), c2.numpy(), atol=1e-12)
+    assert checkpoint_shape(16, (2, 3, 4)) == (1, 2, 2, 3, 4)
+    assert checkpoint_shape(8, (2, 3, 4))[0] == 0 and checkpoint_shape(17, (1, 1, 1))[0] == 2
