@@ -40,14 +40,24 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="compat", choices=["compat", "fixed"])
-    ap.add_argument("--grid", type=int, default=512)
-    ap.add_argument("--frames", type=int, default=300)
+    ap.add_argument("--grid", type=int, default=None, help="default 512 (batched), 1024 (refine)")
+    ap.add_argument("--frames", type=int, default=None, help="default 300 (batched), 1000 (refine)")
+    ap.add_argument("--refine-steps", type=int, default=50)
+    ap.add_argument("--refine-frames", type=int, default=64)
+    ap.add_argument("--refine-trunc", type=float, default=0.04, help="truncation (m) of the refinement volumes")
+    ap.add_argument("--refine-lr", type=float, default=3e-4)
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff"],
+    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff", "refine"],
                     help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames; "
-                         "diff: forward + adjoint timing and finite-difference check at 128^3 x 16 frames")
-    return ap.parse_args()
+                         "diff: forward + adjoint timing and finite-difference check at 128^3 x 16 frames; "
+                         "refine: 1024^3 x 1000 frames 1280x720, then pose refinement of 64 jittered frames")
+    a = ap.parse_args()
+    if a.grid is None:
+        a.grid = 1024 if a.workload == "refine" else 512
+    if a.frames is None:
+        a.frames = 1000 if a.workload == "refine" else 300
+    return a
 
 
 def dist_env():
@@ -180,6 +190,72 @@ def reference_cuda(args, cam, scene, poses, torch, nframes=8):
     wall = float(np.median([m[1] for m in ms]))
     return {"value": nvox / (kern * 1e-3), "unit": UNIT, "kernel_ms_per_frame": kern, "call_ms_per_frame": wall,
             "frames_timed": len(ms), "what": "TSDFVolume::integrate of the reference, one launch + sync per frame"}
+
+
+def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=3):
+    """The same frames in the fixed mode (camera-space SDF, a real surface;
+    the compat field of a camera circling the scene has no zero crossing, so
+    the compat mesh is empty as it is for the reference), then meshes of
+    that field: the engine's fixed-mode marching cubes, the engine's compat
+    marching cubes (the reference's quirks) and the reference's own
+    generate_triangular_surface path (per-layer kernel + host copy loop),
+    all on the same distances."""
+    import ctypes as C
+    from cuphoto import TSDFVolume
+    from cuphoto import _lib as L
+    lib = L.lib()
+    nvox = args.grid ** 3
+    vf = TSDFVolume(volume_cfg(args, cam, "fixed"))
+
+    def integ():
+        vf.reset()
+        vf.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def mesh_timer(vol):
+        n = C.c_int64()
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L.check(lib.gbt_extract_mesh(vol.handle, None, None, 0, 0, C.byref(n), st))
+        cap = max(n.value, 1)
+        verts = torch.empty((cap, 3, 3), dtype=torch.float32, device="cuda")
+        tris = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+        count = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+        def run():
+            L.check(lib.gbt_extract_mesh_async(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
+                                               cap, 0, C.c_void_p(count.data_ptr()), st))
+        ms = timed(run)
+        return {"ms": ms, "triangles": int(n.value), "triangles_per_s": n.value / (ms * 1e-3)}
+
+    t_int = timed(integ)
+    out = {"integrate_voxel_updates_per_s": nvox * len(depths) / (t_int * 1e-3), "integrate_ms": t_int,
+           "mesh_fixed": mesh_timer(vf)}
+    vc = TSDFVolume(volume_cfg(args, cam, "compat"))
+    vc.voxel_distances_data().copy_(vf.voxel_distances_data())
+    out["mesh_compat_same_field"] = mesh_timer(vc)
+    import oracle
+    if oracle.RefHarness.available():
+        r = oracle.RefHarness(volume_cfg(args, cam, "compat"))
+        r.write_distances(vf.voxel_distances_data().cpu().numpy())
+        V, T, ms = r.extract()
+        r.close()
+        out["reference_mesh_same_field"] = {"ms": ms, "triangles": int(len(T)), "triangles_per_s": len(T) / (ms * 1e-3),
+                                            "what": "generate_triangular_surface of the reference: per-layer kernel "
+                                                    "+ sync + host copy loop"}
+    vc.close()
+    vf.close()
+    return out
 
 
 def differentiable_c3(torch, reps=20):
@@ -335,6 +411,156 @@ def differentiable_c3(torch, reps=20):
             "forward_voxel_updates_per_s": nvf / (t_plain * 1e-3),
             "fd_pose": [fd_check("pose", 1e-4), fd_check("pose", 1e-5)], "fd_depth": fd_check("depth", 1e-4),
             "fp32_vs_fp64": fp32_vs_fp64()}
+
+
+def refine_workload(args, torch):
+    """Large pose refinement.  A seeded scene of a ground plane and 20 spheres,
+    `frames` 1280x720 uint16 depth frames (fx = fy = 920) from a circle of
+    cameras; `refine_frames` of them, evenly spaced, get a 1 deg / 5 mm pose
+    error.  (1) Plain forward: the engine's fixed-mode integrate of all
+    frames (jittered ones at their erroneous poses) into a grid^3 volume
+    over the 2.56 m cube, then marching cubes; CUDA-event timed.  (2) The
+    model: the same integrate of the other frames only.  (3) Refinement: for
+    `refine_steps` Adam steps on the jittered frames' se(3) left updates,
+    integrate them (differentiable, FP32, 8-frame recompute chunks) into a
+    fresh volume and minimise the frame-to-model loss
+    L = sum c W (D - D_model)^2 / sum c W, c = [W_model > 0], through the
+    autograd Function (forward + adjoint timed per step).  Reports the
+    rotation, camera-centre and surface-registration errors before and
+    after, and the adjoint's cost against the forward."""
+    import ctypes as C
+    from cuphoto import TSDFVolume, TSDFVolumeConfig
+    from cuphoto import _lib as L
+    from cuphoto import diff as DF
+    from cuphoto import synthetic as S
+    n, nf, nj = args.grid, args.frames, args.refine_frames
+    cam = S.Camera.hd()
+    scene = S.make_scene(7, n_spheres=20)
+    poses = S.circle_poses(nf)
+    frames = S.render_sequence_torch(scene, poses, cam, seed=7)          # (nf, H, W) u16 bits in int16
+    R_true = np.stack([S.matrix_from_quat(p[:4]) for p in poses])
+    t_true = np.stack([p[4:] for p in poses])
+    moved = [int(k) for k in np.linspace(3, nf - 1, nj).round().astype(int)]
+    fixed = [k for k in range(nf) if k not in set(moved)]
+    Rj, tj = S.jitter_poses(R_true, t_true, moved, 1.0, 0.005, seed=17)
+    est = np.stack([S.pose7(Rj[k], tj[k]) for k in range(nf)])
+    depths = [frames[k] for k in range(nf)]
+    tr = args.refine_trunc
+    tc = TSDFVolumeConfig(**S.grid_for(n, 2.56), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy,
+                          camera_width=cam.width, camera_height=cam.height, max_weight=128.0, mode="fixed",
+                          truncation=tr, max_depth=8.0, min_z=0.05)
+    lib = L.lib()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # (1) plain forward + extract, timed (a warm-up pass first)
+    vol = TSDFVolume(tc)
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for it in range(2):
+        e = [ev() for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record()
+        vol.reset()
+        vol.integrate_sequence(depths, est, frames_per_pass=32)
+        e[1].record()
+        n_tris = C.c_int64()
+        L.check(lib.gbt_extract_mesh(vol.handle, None, None, 0, 0, C.byref(n_tris),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        cap = n_tris.value
+        verts = torch.empty((max(cap, 1), 3, 3), dtype=torch.float32, device="cuda")
+        tris = torch.empty((max(cap, 1), 3), dtype=torch.int32, device="cuda")
+        e[1].synchronize()
+        e1b = ev()
+        e1b.record()
+        L.check(lib.gbt_extract_mesh_async(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
+                                           cap, 0, C.c_void_p(count.data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        e[2].record()
+        torch.cuda.synchronize()
+    plain_int_ms = e[0].elapsed_time(e[1])
+    mesh_ms = e1b.elapsed_time(e[2])
+    del verts, tris
+    vol.close()
+    # (2) the model
+    model = TSDFVolume(tc)
+    model.integrate_sequence([depths[k] for k in fixed], est[fixed], frames_per_pass=32)
+    Dm = model.voxel_distances_data()
+    cmask = (model.voxel_weights_data() > 0).to(torch.float32)
+    # the engine's plain integrate of just the jittered frames, for scale
+    v64 = TSDFVolume(tc)
+    torch.cuda.synchronize()
+    e = [ev(), ev()]
+    e[0].record()
+    v64.integrate_sequence([depths[k] for k in moved], est[moved], frames_per_pass=32)
+    e[1].record()
+    torch.cuda.synchronize()
+    plain64_ms = e[0].elapsed_time(e[1])
+    v64.close()
+    # (3) refinement
+    dj = (frames[moved].to(torch.int32) & 0xFFFF).to(torch.float32) * np.float32(0.001)
+    vs = tuple(float(v) for v in model.scale_voxel_size())
+    cfg = DF.DiffConfig((n, n, n), vs, tuple(model.global_offset()), cam.fx, cam.fy, cam.cx, cam.cy,
+                        truncation=tr, max_weight=128.0, max_depth=8.0, min_z=0.05)
+    shape = (n, n, n)
+    D0 = torch.full(shape, tr, dtype=torch.float32, device="cuda")
+    W0 = torch.zeros(shape, dtype=torch.float32, device="cuda")
+    R = torch.as_tensor(Rj[moved], dtype=torch.float32, device="cuda")
+    t = torch.as_tensor(tj[moved], dtype=torch.float32, device="cuda")
+    Rt = torch.as_tensor(R_true[moved], dtype=torch.float32, device="cuda")
+    tt = torch.as_tensor(t_true[moved], dtype=torch.float32, device="cuda")
+
+    def errors(R, t):
+        rot = torch.arccos(torch.clamp((torch.einsum("kij,kij->k", R.double(), Rt.double()) - 1) / 2, -1, 1))
+        cen = ((R.double().transpose(1, 2) @ t.double()[..., None]) -
+               (Rt.double().transpose(1, 2) @ tt.double()[..., None])).squeeze(-1).norm(dim=1)
+        surf = DF.surface_alignment_error(dj, R, t, Rt, tt, cam.fx, cam.fy, cam.cx, cam.cy)
+        return {"rotation_deg": float(torch.rad2deg(rot).mean().item()), "centre_mm": 1e3 * float(cen.mean().item()),
+                "surface_rms_mm": 1e3 * float(surf.mean().item())}
+
+    before = errors(R, t)
+    m = v = None
+    fwd_ms, bwd_ms, losses = [], [], []
+    for it in range(1, args.refine_steps + 1):
+        Rv = R.clone().requires_grad_(True)
+        tv = t.clone().requires_grad_(True)
+        e = [ev() for _ in range(3)]
+        e[0].record()
+        D, W = DF.integrate(dj, Rv, tv, D0, W0, cfg)
+        e[1].record()
+        cw = cmask * W
+        den = cw.sum()
+        loss = (cw * (D - Dm) ** 2).sum() / den
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        fwd_ms.append(e[0].elapsed_time(e[1]))
+        bwd_ms.append(e[1].elapsed_time(e[2]))
+        losses.append(float(loss.item()))
+        g = DF.se3_gradient(Rv.grad.double(), tv.grad.double(), R.double(), t.double())
+        del D, W, cw, den, loss, Rv, tv
+        if m is None:
+            m = torch.zeros_like(g)
+            v = torch.zeros_like(g)
+        m = 0.9 * m + 0.1 * g
+        v = 0.999 * v + 0.001 * g * g
+        xi = -args.refine_lr * (m / (1 - 0.9 ** it)) / ((v / (1 - 0.999 ** it)).sqrt() + 1e-12)
+        R, t = DF.se3_left_update(R, t, xi)
+    after = errors(R, t)
+    f_ms = float(np.median(fwd_ms))
+    b_ms = float(np.median(bwd_ms))
+    return {"workload": "pose refinement: %d^3 voxels of %.2f cm (FP32 D + W = %.1f GB), %d frames 1280x720 uint16, "
+                        "%d jittered frames (1 deg / 5 mm), %d Adam steps" % (n, 256.0 / n, 8 * n ** 3 / 1e9, nf, nj,
+                                                                          args.refine_steps),
+            "truncation_m": tr, "plain_forward": {"integrate_ms": plain_int_ms, "mesh_ms": mesh_ms,
+                                                  "triangles": int(count.item()),
+                                                  "voxel_updates_per_s": n ** 3 * nf / (plain_int_ms * 1e-3)},
+            "plain_integrate_of_jittered_frames_ms": plain64_ms,
+            "refine_step_ms": {"forward": f_ms, "forward_plus_loss_and_adjoint": b_ms,
+                               "fwd_plus_adjoint_over_fwd": (f_ms + b_ms) / f_ms},
+            "loss": {"first": losses[0], "last": losses[-1]},
+            "pose_error_before": before, "pose_error_after": after,
+            "reduction": {k: 1 - after[k] / before[k] for k in before}}
 
 
 def run_reference_arm(args):
@@ -541,6 +767,15 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args)
         return
+    if args.workload == "refine":
+        import torch
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+        eb = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(eb)
+        eb.build()
+        print(json.dumps(refine_workload(args, torch)), flush=True)
+        return
     if args.workload == "diff":
         import torch
         import importlib.util
@@ -714,6 +949,7 @@ def main():
     extras = {}
     if not args.no_extras and world == 1:
         extras["reference_cuda"] = reference_cuda(args, cam, scene, poses, torch)
+        extras["fixed_mode_mesh"] = fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas)
         extras["differentiable"] = differentiable_c3(torch)
         cpu = cpu_baseline(args, cam, scene, poses)
     else:
@@ -722,8 +958,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: seeded plane + 6 spheres, ray-cast uint16 depth, helix trajectory",
-        "config": {"workload": "batched integrate + marching cubes, %d^3 voxels of 0.5 cm, %d frames 640x480 uint16"
-                               % (args.grid, nf),
+        "config": {"workload": "batched integrate + marching cubes, %d^3 voxels of %.2g cm, %d frames 640x480 uint16"
+                               % (args.grid, 256.0 / args.grid, nf),
                    "mode": args.mode, "frames_per_pass": K, "brick": brick, "ctas_per_sm": ctas,
                    "passes_per_step": n_passes, "graph": "reset, integrate passes, mesh captured as CUDA graphs",
                    "l2": "inputs larger than L2: 1 GiB volume + %d MB depth per step" % (frames_dev.numel() * 2 // 2**20),

@@ -248,8 +248,9 @@ constexpr int kBackThreads = 128;
 // independently, so warps with little work do not hold up the others).  The
 // chunk's per-frame (D, W) history sits in shared memory, so the frame loops
 // need no unrolling.  Pose sums: per warp and frame the 12 values are reduced
-// across the warp in T, added into the CTA's shared accumulators in T, and
-// each CTA adds its non-zero totals into grad_pose in double.
+// across the warp in T and added into the CTA's shared accumulators in T;
+// the CTA's last warp to finish adds the non-zero totals into grad_pose in
+// double (no end-of-CTA barrier: finished warps leave at once).
 template <typename T>
 __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, const T* gD_in, const T* gW_in,
                                                                 const T* D0, const T* W0, const T* ckpt,
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
     __shared__ T s_pose[kBatchMaxFrames][12];
     __shared__ T s_acc[kBatchMaxFrames][12];
     __shared__ T s_hist[2 * kChunk][kBackThreads];   // D then W before each frame of the chunk
+    __shared__ int s_done;                           // warps finished
     using O = Ops<T>;
     const int64_t n = (int64_t)g.nx * g.ny * g.nz;
     const int64_t i = blockIdx.x * (int64_t)kBackThreads + threadIdx.x;
@@ -275,6 +277,7 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
     }
     load_poses<T>(g, rot, trans, s_pose);
     for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) s_acc[e / 12][e % 12] = (T)0;
+    if (threadIdx.x == 0) s_done = 0;
     __syncthreads();
     const int64_t frame = (int64_t)g.width * g.height;
     const T M = (T)g.max_weight;
@@ -377,8 +380,14 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
     }
     if (inside && gD0) gD0[i] = gd;
     if (inside && gW0) gW0[i] = gw;
-    __syncthreads();
-    for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) {
+    // the last warp of the CTA to get here flushes the CTA's pose sums
+    __syncwarp();
+    __threadfence_block();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&s_done, 1) == kBackThreads / 32 - 1;
+    if (!__shfl_sync(0xffffffffu, last, 0)) return;
+    __threadfence_block();
+    for (int e = lane; e < g.nframes * 12; e += 32) {
         const double v = (double)s_acc[e / 12][e % 12];
         if (v != 0.0) atomicAdd(grad_pose + e, v);
     }
