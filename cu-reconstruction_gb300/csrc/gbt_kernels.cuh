@@ -62,6 +62,55 @@ __device__ __forceinline__ float compat_cam(float r0, float r1, float r2, float 
     return __fadd_rn(__fmaf_rn(r2, pz, __fmaf_rn(r0, px, __fmul_rn(r1, py))), t);
 }
 
+// Two FP32 values in one 64-bit register pair, for Blackwell's paired FP32
+// instructions (add/mul/fma .rn .f32x2): two IEEE operations per issue slot,
+// each lane rounded exactly as the scalar instruction rounds it.  In the
+// fast-math translation unit the scalar operations flush subnormals, so the
+// paired ones do too.
+#if defined(GBT_REF_ARITH)
+#define GBT_F2_FTZ ".ftz"
+#else
+#define GBT_F2_FTZ ""
+#endif
+struct f2 {
+    unsigned long long r;
+};
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v.r) : "f"(lo), "f"(hi));
+    return v;
+}
+__device__ __forceinline__ f2 f2_splat(float x) { return f2_pack(x, x); }
+__device__ __forceinline__ float f2_lo(f2 v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v.r));
+    return lo;
+}
+__device__ __forceinline__ float f2_hi(f2 v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v.r));
+    return hi;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn" GBT_F2_FTZ ".f32x2 %0, %1, %2, %3;" : "=l"(d.r) : "l"(a.r), "l"(b.r), "l"(c.r));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn" GBT_F2_FTZ ".f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+    return d;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn" GBT_F2_FTZ ".f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+    return d;
+}
+// compat_cam for two voxels of one row (same y, z): r1*y is shared
+__device__ __forceinline__ f2 compat_cam2(float r0, float r2, float t, f2 px, float r1y, float pz) {
+    return f2_add(f2_fma(f2_splat(r2), f2_splat(pz), f2_fma(f2_splat(r0), px, f2_splat(r1y))), f2_splat(t));
+}
+
 #if defined(GBT_REF_ARITH)
 
 __device__ __forceinline__ float centre(int v, float vs, float off) { return ((float)v + 0.5f) * vs + off; }
@@ -72,6 +121,12 @@ __device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) 
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(cz));
     return __fmaf_rn(__fmul_rn(c, f), r, cc);
+}
+__device__ __forceinline__ f2 compat_q2(f2 c, float f, f2 cz, float cc) {
+    float r0, r1;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(f2_lo(cz)));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(f2_hi(cz)));
+    return f2_fma(f2_mul(c, f2_splat(f)), f2_pack(r0, r1), f2_splat(cc));
 }
 __device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
     return ((d * w) + (tsdf * 1.0f)) / nw;
@@ -86,6 +141,10 @@ __device__ __forceinline__ float centre(int v, float vs, float off) {
 }
 __device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) {
     return __fadd_rn(__fdiv_rn(__fmul_rn(c, f), cz), cc);
+}
+__device__ __forceinline__ f2 compat_q2(f2 c, float f, f2 cz, float cc) {
+    const f2 m = f2_mul(c, f2_splat(f));
+    return f2_add(f2_pack(__fdiv_rn(f2_lo(m), f2_lo(cz)), __fdiv_rn(f2_hi(m), f2_hi(cz))), f2_splat(cc));
 }
 __device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
     return __fdiv_rn(__fmaf_rn(d, w, tsdf), nw);
@@ -244,20 +303,30 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
     if (MODE == kCompat) {
         const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
         const float r6 = pr[6], r7 = pr[7], r8 = pr[8], t0 = pr[9], t1 = pr[10], t2 = pr[11];
+        // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51) for the
+        // thread's 4 voxels, two at a time in paired FP32; a voxel with world
+        // z == 0 or camera z == 0 maps to pixel (0, 0)
+        const float m0 = __fmul_rn(r1, py), m1 = __fmul_rn(r4, py), m2 = __fmul_rn(r7, py);
+        int pu[4], pv[4];
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            const f2 X = f2_pack(px[h], px[h + 1]);
+            const f2 cxv = compat_cam2(r0, r2, t0, X, m0, pz);
+            const f2 cyv = compat_cam2(r3, r5, t1, X, m1, pz);
+            const f2 czv = compat_cam2(r6, r8, t2, X, m2, pz);
+            const f2 qu = compat_q2(cxv, v.fx, czv, v.cx);
+            const f2 qv = compat_q2(cyv, v.fy, czv, v.cy);
+            const bool ok0 = pz != 0.f && f2_lo(czv) != 0.f;
+            const bool ok1 = pz != 0.f && f2_hi(czv) != 0.f;
+            pu[h] = ok0 ? (int)f2_lo(qu) : 0;
+            pv[h] = ok0 ? (int)f2_lo(qv) : 0;
+            pu[h + 1] = ok1 ? (int)f2_hi(qu) : 0;
+            pv[h + 1] = ok1 ? (int)f2_hi(qv) : 0;
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (i >= nvalid) break;
-            // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51)
-            int u = 0, vv = 0;
-            if (pz != 0.f) {
-                const float cxv = compat_cam(r0, r1, r2, t0, px[i], py, pz);
-                const float cyv = compat_cam(r3, r4, r5, t1, px[i], py, pz);
-                const float czv = compat_cam(r6, r7, r8, t2, px[i], py, pz);
-                if (czv != 0.f) {
-                    u = (int)compat_q(cxv, v.fx, czv, v.cx);
-                    vv = (int)compat_q(cyv, v.fy, czv, v.cy);
-                }
-            }
+            const int u = pu[i], vv = pv[i];
             // tsdf_volume.cu:166-187
             if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
             const char* row = dimg + (int64_t)vv * pitch;
@@ -587,32 +656,46 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
             }
             const int total = __shfl_sync(0xffffffffu, x, 31);
             if (lane < kParts) s_wsum[lane] = x - s;
-            if (lane == 0) {
-                // decoupled look-back over the preceding tiles
-                long long prefix = 0;
-                if (tile == 0) {
-                    st_release(a.status + tile, kFlagIncl | (unsigned long long)total);
-                } else {
-                    st_release(a.status + tile, kFlagAgg | (unsigned long long)total);
-                    int64_t j = (int64_t)tile - 1;
-                    int spins = 0;
-                    while (j >= 0) {
-                        const unsigned long long w = ld_acquire(a.status + j);
-                        const unsigned long long flag = w & ~kValueMask;
-                        if (flag == 0ull) {
-                            if (++spins > kLookbackSpinLimit) {
-                                atomicExch(a.error, 1);
-                                break;
-                            }
-                            __nanosleep(64);
-                            continue;
+            // decoupled look-back over the preceding tiles, 32 at a time: lane
+            // l reads tile (j - l); the nearest tile with an inclusive prefix
+            // ends the walk, the aggregates before it are summed by the warp
+            long long prefix = 0;
+            if (tile == 0) {
+                if (lane == 0) st_release(a.status + tile, kFlagIncl | (unsigned long long)total);
+            } else {
+                if (lane == 0) st_release(a.status + tile, kFlagAgg | (unsigned long long)total);
+                int64_t j = (int64_t)tile - 1;
+                int spins = 0;
+                bool failed = false;
+                while (j >= 0) {
+                    const int64_t mine = j - lane;
+                    unsigned long long w = mine >= 0 ? ld_acquire(a.status + mine) : kFlagIncl;
+                    // wait until every tile of the window has published something
+                    while (__any_sync(0xffffffffu, (w & ~kValueMask) == 0ull)) {
+                        if (++spins > kLookbackSpinLimit) {
+                            failed = true;
+                            break;
                         }
-                        prefix += (long long)(w & kValueMask);
-                        if (flag == kFlagIncl) break;
-                        --j;
+                        __nanosleep(64);
+                        if ((w & ~kValueMask) == 0ull) w = ld_acquire(a.status + mine);
                     }
+                    if (failed) break;
+                    const unsigned incl_lanes = __ballot_sync(0xffffffffu, (w & ~kValueMask) == kFlagIncl);
+                    const int stop = incl_lanes ? __ffs(incl_lanes) - 1 : 31;   // nearest inclusive tile
+                    long long v = lane <= stop ? (long long)(w & kValueMask) : 0;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    prefix += v;
+                    if (incl_lanes) break;
+                    j -= 32;
+                }
+                if (failed) {
+                    if (lane == 0) atomicExch(a.error, 1);
+                } else if (lane == 0) {
                     st_release(a.status + tile, kFlagIncl | (unsigned long long)(prefix + total));
                 }
+            }
+            if (lane == 0) {
                 s_prefix = prefix;
                 if (tile == a.ntiles - 1) *a.total = prefix + total;
             }
