@@ -27,6 +27,7 @@ UNITS = {
     "capi.cu": [],
     "k_noalloc.cu": [],
     "k_diff.cu": [],
+    "k_points.cu": [],
 }
 
 

@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "compat_geom.cuh"
 #include "gbt_internal.h"
 
 #ifndef GBT_ARITH_NS
@@ -34,33 +35,8 @@ enum { kCompat = 0, kFixed = 1 };
 // Arithmetic of the compat mode.  It follows the reference operation for
 // operation (se3.cuh:125-140,165-175,207-223; camera_util.cu:15-16;
 // tsdf_volume.cu:117-119,183; marching_cubes.cu:43-48) because the compat mode
-// must reproduce its results bit for bit.
-//
-// The rotation entries and the R*p+t rows are written with explicit
-// intrinsics in both arithmetics, in the rounding order of the reference's
-// own build: every entry fuses its first product except R00 = 1-(yy+zz),
-// which rounds both products; each row is fma(r2, z, fma(r0, x, r1*y)) + t.
-// That order was measured against the reference's kernels on 5.4M voxel
-// projections (pixel index decoded from a coded depth image), where it is
-// the only one of the tried orders without a single differing pixel.
-
-__device__ __forceinline__ void compat_rotation(const float* q, float* R) {
-    const float x = __fmul_rn(2.f, q[0]), y = __fmul_rn(2.f, q[1]), z = __fmul_rn(2.f, q[2]);
-    const float wx = __fmul_rn(x, q[3]), wy = __fmul_rn(y, q[3]), wz = __fmul_rn(z, q[3]);
-    const float xx = __fmul_rn(x, q[0]), yy = __fmul_rn(y, q[1]), zz = __fmul_rn(z, q[2]);
-    R[0] = __fsub_rn(1.f, __fadd_rn(yy, zz));
-    R[1] = __fmaf_rn(y, q[0], -wz);
-    R[2] = __fmaf_rn(z, q[0], wy);
-    R[3] = __fmaf_rn(y, q[0], wz);
-    R[4] = __fsub_rn(1.f, __fmaf_rn(x, q[0], zz));
-    R[5] = __fmaf_rn(z, q[1], -wx);
-    R[6] = __fmaf_rn(z, q[0], -wy);
-    R[7] = __fmaf_rn(z, q[1], wx);
-    R[8] = __fsub_rn(1.f, __fmaf_rn(x, q[0], yy));
-}
-__device__ __forceinline__ float compat_cam(float r0, float r1, float r2, float t, float px, float py, float pz) {
-    return __fadd_rn(__fmaf_rn(r2, pz, __fmaf_rn(r0, px, __fmul_rn(r1, py))), t);
-}
+// must reproduce its results bit for bit.  The rotation and the R*p+t rows
+// are in compat_geom.cuh (shared with the point-cloud kernels).
 
 // Two FP32 values in one 64-bit register pair, for Blackwell's paired FP32
 // instructions (add/mul/fma .rn .f32x2): two IEEE operations per issue slot,

@@ -91,6 +91,7 @@ class BatchItem(C.Structure):
 
 MAX_FRAMES_PER_SCENE_PASS = 128
 DIFF_CHUNK_FRAMES = 8
+POINT_BYTES = 33   # gbt_point, the reference's packed cudaPointCloud::Vertex
 
 # (name, restype, argtypes) of every exported entry point, in header order.
 SIGNATURES = [
@@ -116,6 +117,15 @@ SIGNATURES = [
                                          C.c_void_p, C.c_void_p]),
     ("gbt_extract_mesh_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                            C.c_void_p, C.c_void_p]),
+    ("gbt_points_extract", C.c_int, [C.POINTER(C.c_double * 9), C.c_void_p, C.c_int64, C.c_int32, C.c_float,
+                                     C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(C.c_double * 7),
+                                     C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("gbt_points_transform", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double * 7), C.c_void_p]),
+    ("gbt_points_project", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double * 9), C.POINTER(C.c_double * 7),
+                                     C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
+                                     C.c_void_p, C.c_void_p]),
+    ("gbt_image_filter_if", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_float,
+                                      C.c_void_p]),
     ("gbt_last_error", C.c_char_p, []),
     ("gbt_version", C.c_char_p, []),
 ]

@@ -281,6 +281,72 @@ gbt_status gbt_extract_mesh_async(gbt_volume* vol, float* verts, int32_t* tris, 
 gbt_status gbt_extract_mesh_noalloc(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                     int64_t index_base, int64_t* d_n_tris, void* stream);
 
+/* ---- Point clouds ---------------------------------------------------------
+ * The reference's cudaPointCloud (cuda_point_cloud.cuh:13-103,
+ * cuda_point_cloud.cu:22-385): depth back-projection, rigid transform, and
+ * the z-buffer projection that turns a cloud into the colour + depth images
+ * integrate takes.  Arithmetic as the reference's: back-projection in double
+ * rounded to float; poses as float quaternion + translation applied as the
+ * TSDF kernels apply them; pixels by truncation of (x*fx)/z + c.
+ *
+ * camera_matrix: the reference's std::array<double, 9>, read as the
+ * reference reads it, which differs between the two directions:
+ *   back-projection (point_cloud_extract, :44-47): fx = m[0], fy = m[4],
+ *     cx = m[6], cy = m[7]  (the array holds a column-major 3x3);
+ *   projection (project_to_depth / project_to_color_depth, :248-251, :311-314):
+ *     fx = m[0], fy = m[4], cx = m[2], cy = m[5]  (row-major). */
+
+/* cudaPointCloud::Vertex (cuda_point_cloud.cuh:17-28): packed, 33 bytes. */
+#pragma pack(push, 1)
+typedef struct {
+    float pos[3];
+    float normal[4];
+    uint8_t color[3];
+    uint16_t class_id;
+} gbt_point;
+#pragma pack(pop)
+
+/* Replaces point_cloud_extract + cudaPointCloud::extract_points
+ * (cuda_point_cloud.cu:23-70,179-226).  For every pixel (x, y) with depth > 0
+ * writes points[start_index + y*width + x] = {R*p + t, normal 0, colour, class 0}
+ * with p = ((x - cx) d / fx, (y - cy) d / fy, d); pixels with depth <= 0 leave
+ * their slot untouched.  depth: float32 metres or uint16 (GBT_DEPTH_*, times
+ * depth_scale), pitched; color_rgb8: 3 bytes per pixel, pitched, or NULL for
+ * white points.  pose {qw,qx,qy,qz,tx,ty,tz}.  Returns GBT_ERR_CAPACITY
+ * (nothing written) when start_index + width*height > capacity: the
+ * reference writes past a too-small cloud. */
+gbt_status gbt_points_extract(const double camera_matrix[9], const void* depth, int64_t depth_pitch_bytes,
+                              int32_t depth_format, float depth_scale, const uint8_t* color_rgb8,
+                              int64_t color_pitch_bytes, int32_t width, int32_t height, const double pose[7],
+                              int64_t start_index, gbt_point* points, int64_t capacity, void* stream);
+
+/* Replaces transform_points + cudaPointCloud::transform
+ * (cuda_point_cloud.cu:73-86,356-385): pos = R*pos + t for n points. */
+gbt_status gbt_points_transform(gbt_point* points, int64_t n, const double pose[7], void* stream);
+
+/* Bytes of scratch gbt_points_project needs for a width x height image. */
+#define GBT_POINTS_PROJECT_SCRATCH_BYTES(width, height) ((size_t)(width) * (size_t)(height) * 8u)
+
+/* Replaces cudaPointCloud::project_to_depth / project_to_color_depth
+ * (cuda_point_cloud.cu:229-353), whose z-buffer is a host loop, with a GPU
+ * z-buffer that gives the same images: each point goes through pose, lands on
+ * pixel ((int)((x fx)/z + cx), (int)((y fy)/z + cy)) unless z == 0 or the
+ * pixel is outside the image, and a pixel keeps the point of smallest z, the
+ * lowest point index among equal z (the loop's first-wins order); negative z
+ * is not rejected (as in the reference).  depth receives that z, 0 where no
+ * point landed (filter_image_if of FLT_MAX to 0); color_rgb8 (NULL: depth
+ * only) the point's colour, 0 where none.  scratch: device memory of
+ * GBT_POINTS_PROJECT_SCRATCH_BYTES(width, height).  n < 2^32. */
+gbt_status gbt_points_project(const gbt_point* points, int64_t n, const double camera_matrix[9], const double pose[7],
+                              float* depth, int64_t depth_pitch_bytes, uint8_t* color_rgb8, int64_t color_pitch_bytes,
+                              int32_t width, int32_t height, void* scratch, void* stream);
+
+/* Replaces filter_image_if (cuda_point_cloud.cu:89-99): pixels with
+ * |value - filter_value| < 1e-10 (util.cu:6-10) become set_value. */
+gbt_status gbt_image_filter_if(float* image, int64_t pitch_bytes, int32_t width, int32_t height, float filter_value,
+                               float set_value, void* stream);
+
+
 /* Message for the last failure on the calling thread ("" if none). */
 const char* gbt_last_error(void);
 

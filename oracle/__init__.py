@@ -202,6 +202,61 @@ def diff_backward(cfg, grad_D, grad_W, D0, W0, depth, rot, trans):
 
 
 # ---------------------------------------------------------------------------
+# Point clouds (cuda_point_cloud.cu).  A cloud is an (n, 33) uint8 array of
+# the reference's packed vertices; POINT_DTYPE views it field by field.
+POINT_DTYPE = np.dtype([("pos", "<f4", 3), ("normal", "<f4", 4), ("color", "u1", 3), ("class_id", "<u2")])
+assert POINT_DTYPE.itemsize == 33
+
+
+def _points_lib():
+    so = lib()
+    if not getattr(so, "_points_ready", False):
+        vp = C.c_void_p
+        so.oracle_points_extract.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int64, vp]
+        so.oracle_points_transform.argtypes = [vp, C.c_int64, vp]
+        so.oracle_points_project.argtypes = [vp, C.c_int64, vp, vp, C.c_int32, C.c_int32, vp, vp]
+        so.oracle_filter_if.argtypes = [vp, C.c_int64, C.c_float, C.c_float]
+        so._points_ready = True
+    return so
+
+
+def points_extract(K9, depth, rgb, pose, points, start=0):
+    """In place on points ((n, 33) uint8): the pixels with depth > 0."""
+    depth = np.ascontiguousarray(depth, np.float32)
+    H, W = depth.shape
+    K9 = np.ascontiguousarray(K9, np.float64)
+    pose = np.ascontiguousarray(pose, np.float64)
+    rgb = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+    assert points.dtype == np.uint8 and points.flags.c_contiguous and points.size >= (start + W * H) * 33
+    _points_lib().oracle_points_extract(_p(K9), _p(depth), None if rgb is None else _p(rgb), W, H, _p(pose),
+                                        start, _p(points))
+    return points
+
+
+def points_transform(points, pose):
+    pose = np.ascontiguousarray(pose, np.float64)
+    _points_lib().oracle_points_transform(_p(points), points.size // 33, _p(pose))
+    return points
+
+
+def points_project(points, K9, pose, W, H, color=True):
+    """(depth (H, W) float32, rgb (H, W, 3) uint8 or None)."""
+    K9 = np.ascontiguousarray(K9, np.float64)
+    pose = np.ascontiguousarray(pose, np.float64)
+    depth = np.empty((H, W), np.float32)
+    rgb = np.empty((H, W, 3), np.uint8) if color else None
+    _points_lib().oracle_points_project(_p(points), points.size // 33, _p(K9), _p(pose), W, H, _p(depth),
+                                        None if rgb is None else _p(rgb))
+    return depth, rgb
+
+
+def filter_if(img, filter_value, set_value):
+    img = np.ascontiguousarray(img, np.float32).copy()
+    _points_lib().oracle_filter_if(_p(img), img.size, filter_value, set_value)
+    return img
+
+
+# ---------------------------------------------------------------------------
 class RefHarness:
     """The reference's own kernels (compiled from its sources) driven with its
     host-side logic.  Needs a GPU and oracle/_ref/ref_tsdf.cubin."""
@@ -228,6 +283,9 @@ class RefHarness:
             so.ref_write_distances.argtypes = [vp, vp]
             so.ref_extract.argtypes = [vp, vp, vp, i64, C.POINTER(f)]
             so.ref_extract.restype = i64
+            so.ref_points_extract.argtypes = [vp, vp, C.c_size_t, i32, i32, vp, C.c_size_t, vp, i64, vp]
+            so.ref_points_transform.argtypes = [vp, C.c_uint32, vp]
+            so.ref_filter_if.argtypes = [vp, C.c_size_t, i32, i32, f, f]
             if so.ref_load(REF_CUBIN.encode(), REF_NAMES.encode()) != 0:
                 raise RuntimeError("reference kernels: " + so.ref_last_error().decode())
             cls._so = so
@@ -257,6 +315,27 @@ class RefHarness:
     @property
     def truncation(self):
         return self.lib().ref_truncation(self.h)
+
+    # -- the reference's point-cloud kernels (device pointers in and out) -----
+    @classmethod
+    def points_extract(cls, K9, depth_ptr, pitch, width, height, color_ptr, color_pitch, pose, start, points_ptr):
+        K9 = np.ascontiguousarray(K9, np.float64)
+        p = np.ascontiguousarray(pose, np.float64)
+        if cls.lib().ref_points_extract(_p(K9), C.c_void_p(depth_ptr), pitch, width, height,
+                                        C.c_void_p(color_ptr) if color_ptr else None, color_pitch, _p(p), start,
+                                        C.c_void_p(points_ptr)) != 0:
+            raise RuntimeError(cls.lib().ref_last_error().decode())
+
+    @classmethod
+    def points_transform(cls, points_ptr, n, pose):
+        p = np.ascontiguousarray(pose, np.float64)
+        if cls.lib().ref_points_transform(C.c_void_p(points_ptr), n, _p(p)) != 0:
+            raise RuntimeError(cls.lib().ref_last_error().decode())
+
+    @classmethod
+    def filter_if(cls, img_ptr, pitch, width, height, filter_value, set_value):
+        if cls.lib().ref_filter_if(C.c_void_p(img_ptr), pitch, width, height, filter_value, set_value) != 0:
+            raise RuntimeError(cls.lib().ref_last_error().decode())
 
     def integrate(self, depth_ptr, pitch, width, height, pose):
         """depth_ptr: device float32 metres.  Returns the kernel time in ms."""

@@ -8,7 +8,7 @@ Outputs
   oracle/_build/libref_harness.so  host driver for the reference's kernels
   oracle/_ref/ref_tsdf.cubin       the reference's kernels, compiled from
                                    modules/src/cuda/{tsdf_volume,marching_cubes,
-                                   camera_util}.cu with the reference's own
+                                   camera_util,cuda_point_cloud,util}.cu with the reference's own
                                    device flags (-use_fast_math -rdc=true,
                                    modules/CMakeLists.txt:17-22,73,79), linked
   oracle/_ref/ref_kernels.txt      mangled names of its kernels, read from the
@@ -16,8 +16,9 @@ Outputs
 
 The reference cubin is only built where the reference checkout exists
 (REFERENCE_ROOT, default /root/reference); elsewhere a cubin built earlier is
-used if present.  OpenCV is not installed, so ref_shim/ supplies the two
-image-view types the reference's headers name.
+used if present.  OpenCV is not installed, so ref_shim/ supplies the
+image-view types the reference's headers name and declarations of the host
+image type its point-cloud source uses (only its kernels are compiled).
 """
 import os
 import shutil
@@ -30,8 +31,13 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-REF_UNITS = ["tsdf_volume", "marching_cubes", "camera_util"]
-REF_KERNELS = ["cu_tsdf_integrate", "set_array_to_value", "init_voxel_transofrmation", "marching_cubes_kernel"]
+REF_UNITS = ["tsdf_volume", "marching_cubes", "camera_util", "cuda_point_cloud", "util"]
+# key -> a substring of the kernel's mangled name
+REF_KERNELS = {"cu_tsdf_integrate": "cu_tsdf_integrate", "set_array_to_value": "set_array_to_value",
+               "init_voxel_transofrmation": "init_voxel_transofrmation",
+               "marching_cubes_kernel": "marching_cubes_kernel",
+               "point_cloud_extract": "point_cloud_extractILb0E", "point_cloud_extract_rgb": "point_cloud_extractILb1E",
+               "transform_points": "transform_points", "filter_image_if": "filter_image_if"}
 
 
 def _run(cmd):
@@ -87,7 +93,8 @@ def build_reference_cubin(force=False):
     if not os.path.isdir(os.path.join(REF_ROOT, "modules")):
         return cubin if os.path.exists(cubin) and os.path.exists(names_file) else None
     srcs = [os.path.join(REF_ROOT, "modules/src/cuda/%s.cu" % u) for u in REF_UNITS]
-    if not force and not _stale(cubin, srcs + [__file__]) and os.path.exists(names_file):
+    shims = [os.path.join(HERE, "ref_shim/opencv2/core/core.hpp"), os.path.join(HERE, "ref_shim/opencv2/core/cuda/common.hpp")]
+    if not force and not _stale(cubin, srcs + shims + [__file__]) and os.path.exists(names_file):
         return cubin
     os.makedirs(REF_OUT, exist_ok=True)
     nvcc = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -104,8 +111,8 @@ def build_reference_cubin(force=False):
     os.replace(cubin + ".tmp", cubin)
     syms = _elf_symbols(cubin)
     with open(names_file, "w") as f:
-        for k in REF_KERNELS:
-            hits = [s for s in syms if ("cuphoto" in s and k in s and s.startswith("_Z"))]
+        for k, pat in REF_KERNELS.items():
+            hits = [s for s in syms if ("cuphoto" in s and pat in s and s.startswith("_Z"))]
             if not hits:
                 raise RuntimeError("kernel %s not found in the reference cubin" % k)
             f.write("%s %s\n" % (k, sorted(hits, key=len)[0]))
@@ -116,7 +123,8 @@ def build_ref_harness(force=False):
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "ref_harness.cpp")
     out = os.path.join(BUILD, "libref_harness.so")
-    if force or _stale(out, [src, __file__, os.path.join(HERE, "ref_shim/opencv2/core/cuda/common.hpp")]):
+    if force or _stale(out, [src, __file__, os.path.join(HERE, "ref_shim/opencv2/core/cuda/common.hpp"),
+                             os.path.join(HERE, "ref_shim/opencv2/core/core.hpp")]):
         _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src,
               "-I" + os.path.join(HERE, "ref_shim"), "-I" + os.path.join(CUDA_HOME, "include"),
               "-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart_static", "-ldl", "-lpthread", "-lrt",

@@ -10,6 +10,9 @@
 //   TSDFVolume::integrate                 tsdf_volume.cu:257-290
 //   generate_triangular_surface           marching_cubes.cu:191-237
 //   copy_data_mesh_to_host                marching_cubes.cu:159-189
+//   cudaPointCloud::extract_points        cuda_point_cloud.cu:179-226
+//   cudaPointCloud::transform             cuda_point_cloud.cu:356-385
+//   filter_image_if launches              cuda_point_cloud.cu:273-278
 //
 // It is used to pin the CPU oracle and the engine against the reference's
 // real GPU results, and to time the reference's integrate on the same GPU.
@@ -296,6 +299,68 @@ int64_t ref_extract(ref_volume* v, float* verts_out, int32_t* tris_out, int64_t 
         }
     }
     return T;
+}
+
+// cudaPointCloud::extract_points (cuda_point_cloud.cu:179-226): the camera
+// matrix goes to the kernels' __device__ double K[3][3] (cudaMemcpyToSymbol
+// there), 8x8 blocks, point_cloud_extract<true> when a colour image is given.
+// points: device memory of the reference's 33-byte vertices.
+int ref_points_extract(const double* K9, const float* depth, size_t pitch, int width, int height,
+                       const unsigned char* color, size_t color_pitch, const double* T, int64_t start, void* points) {
+    const char* key = color ? "point_cloud_extract_rgb" : "point_cloud_extract";
+    if (!g_k.count(key)) {
+        g_err = "point-cloud kernels are not in the reference cubin";
+        return 1;
+    }
+    void* kp = nullptr;
+    size_t ksz = 0;
+    cudaError_t e = cudaLibraryGetGlobal(&kp, &ksz, g_lib, "_ZN7cuphoto1KE");
+    if (e != cudaSuccess) return fail("cudaLibraryGetGlobal K", e);
+    if (ksz != 9 * sizeof(double)) {
+        g_err = "unexpected size of the reference's K";
+        return 1;
+    }
+    e = cudaMemcpy(kp, K9, ksz, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail("cudaMemcpy K", e);
+    cv::cuda::PtrStepSzf d(height, width, const_cast<float*>(depth), pitch);
+    cv::cuda::PtrStepb c(const_cast<unsigned char*>(color), color_pitch);
+    float4 quat = make_float4(T[1], T[2], T[3], T[0]);
+    float3 trans = make_float3(T[4], T[5], T[6]);
+    int64_t start_idx = start;
+    void* args[] = {&d, &c, &quat, &trans, &start_idx, &points};
+    const dim3 block(8, 8, 1), grid(idiv_up(width, 8), idiv_up(height, 8), 1);
+    e = cudaLaunchKernel((const void*)g_k[key], grid, block, args, 0, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? 0 : fail("point_cloud_extract", e);
+}
+
+// cudaPointCloud::transform (cuda_point_cloud.cu:356-385): 16-thread blocks.
+int ref_points_transform(void* points, uint32_t n, const double* T) {
+    if (!g_k.count("transform_points")) {
+        g_err = "point-cloud kernels are not in the reference cubin";
+        return 1;
+    }
+    float4 quat = make_float4(T[1], T[2], T[3], T[0]);
+    float3 trans = make_float3(T[4], T[5], T[6]);
+    uint32_t num = n;
+    void* args[] = {&quat, &trans, &num, &points};
+    cudaError_t e = cudaLaunchKernel((const void*)g_k["transform_points"], dim3(idiv_up(n, 16)), dim3(16), args, 0, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? 0 : fail("transform_points", e);
+}
+
+// filter_image_if as project_to_depth launches it (cuda_point_cloud.cu:273-278).
+int ref_filter_if(float* img, size_t pitch, int width, int height, float filter_value, float set_value) {
+    if (!g_k.count("filter_image_if")) {
+        g_err = "point-cloud kernels are not in the reference cubin";
+        return 1;
+    }
+    cv::cuda::PtrStepSzf d(height, width, img, pitch);
+    void* args[] = {&d, &filter_value, &set_value};
+    const dim3 block(8, 8, 1), grid(idiv_up(width, 8), idiv_up(height, 8), 1);
+    cudaError_t e = cudaLaunchKernel((const void*)g_k["filter_image_if"], grid, block, args, 0, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? 0 : fail("filter_image_if", e);
 }
 
 }  // extern "C"

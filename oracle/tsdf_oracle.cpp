@@ -13,6 +13,9 @@
 //   volume set-up      tsdf_volume.cu:194-212,227-254 (voxel size, truncation, init)
 //   compat mesh        marching_cubes.cu:23-157 (per-cube classification and
 //                      edge interpolation) + :159-237 (layer loop, host assembly)
+//   point clouds       cuda_point_cloud.cu:22-99 (point_cloud_extract,
+//                      transform_points, filter_image_if) + :292-353 (the host
+//                      z-buffer loop of project_to_color_depth)
 //
 // The reference is compiled with -use_fast_math, so its divisions are the
 // GPU's approximate divide.  The oracle does NOT imitate that: every division
@@ -28,6 +31,7 @@
 // restated here operation for operation as the engine defines it.
 //
 // Build with -ffp-contract=off so the compiler adds no contraction of its own.
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -741,6 +745,104 @@ void oracle_diff_backward(const oracle_diff_cfg* g, const double* grad_D, const 
         if (grad_D0) grad_D0[i] = gd;
         if (grad_W0) grad_W0[i] = gw;
     }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Point clouds: cudaPointCloud (cuda_point_cloud.cu:22-385) restated.  A point
+// is the reference's packed 33-byte Vertex (cuda_point_cloud.cuh:17-28):
+// float pos[3], float normal[4], uint8 color[3], uint16 classID.
+namespace {
+
+constexpr int kPointBytes = 33;
+
+inline void point_pos(const uint8_t* pt, float* p) { std::memcpy(p, pt, 12); }
+
+inline void pose_apply(const CompatPose& P, const float* p, float* out) {
+    out[0] = rot_row(P.R.r + 0, p[0], p[1], p[2], P.t[0]);
+    out[1] = rot_row(P.R.r + 3, p[0], p[1], p[2], P.t[1]);
+    out[2] = rot_row(P.R.r + 6, p[0], p[1], p[2], P.t[2]);
+}
+
+}  // namespace
+
+extern "C" {
+
+// point_cloud_extract (cuda_point_cloud.cu:22-70): K as the kernel reads it
+// (K[0][0], K[1][1], K[2][0], K[2][1] of the double[3][3] copied from the
+// 9-array: m[0], m[4], m[6], m[7]); back-projection in double
+// ((float)x - cx) * d / fx, rounded to float; pixels with depth <= 0 leave
+// their slot untouched; colour rgb or white.  depth: W*H float metres.
+void oracle_points_extract(const double* m, const float* depth, const uint8_t* rgb, int32_t W, int32_t H,
+                           const double* pose, int64_t start, uint8_t* points) {
+    const CompatPose P = compat_pose(pose);
+    const double fx = m[0], fy = m[4], cx = m[6], cy = m[7];
+    for (int32_t y = 0; y < H; ++y)
+        for (int32_t x = 0; x < W; ++x) {
+            const float d = depth[(int64_t)y * W + x];
+            if (d <= 0.0f) continue;
+            const float p[3] = {(float)((((double)(float)x) - cx) * (double)d / fx),
+                                (float)((((double)(float)y) - cy) * (double)d / fy), d};
+            float w[7] = {0, 0, 0, 0, 0, 0, 0};
+            pose_apply(P, p, w);
+            uint8_t* dst = points + (start + (int64_t)y * W + x) * kPointBytes;
+            std::memcpy(dst, w, 28);
+            const uint8_t* c = rgb ? rgb + ((int64_t)y * W + x) * 3 : nullptr;
+            dst[28] = c ? c[0] : 255;
+            dst[29] = c ? c[1] : 255;
+            dst[30] = c ? c[2] : 255;
+            dst[31] = 0;
+            dst[32] = 0;
+        }
+}
+
+// transform_points (cuda_point_cloud.cu:73-86).
+void oracle_points_transform(uint8_t* points, int64_t n, const double* pose) {
+    const CompatPose P = compat_pose(pose);
+    for (int64_t i = 0; i < n; ++i) {
+        float p[3], w[3];
+        point_pos(points + i * kPointBytes, p);
+        pose_apply(P, p, w);
+        std::memcpy(points + i * kPointBytes, w, 12);
+    }
+}
+
+// project_to_color_depth (cuda_point_cloud.cu:292-353): the host z-buffer
+// loop in point order, then filter_image_if(FLT_MAX -> 0).  K read as
+// m[0], m[4], m[2], m[5].  The pixel is (int)((x*fx)/z + cx) in float; a
+// non-finite value is dropped.  rgb may be NULL (project_to_depth).
+void oracle_points_project(const uint8_t* points, int64_t n, const double* m, const double* pose, int32_t W,
+                           int32_t H, float* depth, uint8_t* rgb) {
+    const CompatPose P = compat_pose(pose);
+    const float fx = (float)m[0], fy = (float)m[4], cx = (float)m[2], cy = (float)m[5];
+    for (int64_t i = 0; i < (int64_t)W * H; ++i) depth[i] = FLT_MAX;
+    if (rgb) std::memset(rgb, 0, (size_t)W * H * 3);
+    for (int64_t i = 0; i < n; ++i) {
+        const uint8_t* pt = points + i * kPointBytes;
+        float p[3], c[3];
+        point_pos(pt, p);
+        pose_apply(P, p, c);
+        if (c[2] == 0.f) continue;
+        const float qu = (c[0] * fx) / c[2] + cx;
+        const float qv = (c[1] * fy) / c[2] + cy;
+        if (qu != qu || qv != qv) continue;
+        const int32_t u = f2i_rz_sat(qu), v = f2i_rz_sat(qv);
+        if (u < 0 || u >= W || v < 0 || v >= H) continue;
+        float& dv = depth[(int64_t)v * W + u];
+        if (dv > c[2]) {
+            dv = c[2];
+            if (rgb) std::memcpy(rgb + ((int64_t)v * W + u) * 3, pt + 28, 3);
+        }
+    }
+    for (int64_t i = 0; i < (int64_t)W * H; ++i)
+        if (std::fabs(depth[i] - FLT_MAX) < 1e-10f) depth[i] = 0.0f;
+}
+
+// filter_image_if (cuda_point_cloud.cu:89-99) with near_equal (util.cu:6-10).
+void oracle_filter_if(float* img, int64_t n, float filter_value, float set_value) {
+    for (int64_t i = 0; i < n; ++i)
+        if (std::fabs(img[i] - filter_value) < 1e-10f) img[i] = set_value;
 }
 
 }  // extern "C"
