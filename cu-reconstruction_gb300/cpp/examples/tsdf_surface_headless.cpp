@@ -13,6 +13,10 @@
 //
 // --sequence integrates N frames with their own world-to-camera poses
 // (N x 7 doubles: qw qx qy qz tx ty tz) through the multi-frame driver.
+// --points goes through a point cloud instead of the depth image: the frame
+// is back-projected into a cudaPointCloud at the inverse of the configured
+// pose (world coordinates), optionally stored with save_ply (--points_ply),
+// and reconstruct_surface(cloud) projects it back and integrates it.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -30,6 +34,12 @@ std::string arg(int argc, char** argv, const char* name, const char* def) {
     for (int i = 1; i + 1 < argc; ++i)
         if (std::strcmp(argv[i], name) == 0) return argv[i + 1];
     return def;
+}
+
+bool flag(int argc, char** argv, const char* name) {
+    for (int i = 1; i < argc; ++i)
+        if (std::strcmp(argv[i], name) == 0) return true;
+    return false;
 }
 
 bool read_file(const std::string& path, std::vector<char>& out) {
@@ -68,7 +78,25 @@ int main(int argc, char** argv) {
             const std::array<double, 7> pose = tsdf.global_pose();
             std::printf("pose %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", pose[0], pose[1], pose[2], pose[3],
                         pose[4], pose[5], pose[6]);
-            tsdf.reconstruct_surface(rgb, depth);
+            if (flag(argc, argv, "--points")) {
+                const double fx = cfg.get<float>("camera.fx"), fy = cfg.get<float>("camera.fy");
+                const double cx = cfg.get<float>("camera.cx"), cy = cfg.get<float>("camera.cy");
+                // cx, cy at both places the cloud reads them (column- and row-major)
+                const std::array<double, 9> K{fx, 0, cx, 0, fy, cy, cx, cy, 1};
+                auto cloud = cuphoto::cudaPointCloud::create(K, (size_t)width * height);
+                const cuphoto::SE3 inv = tsdf.get_global_transformation().inverse();
+                const cuphoto::Quat q(inv.rotationMatrix());
+                const cuphoto::Vec3 t = inv.translation();
+                const std::array<double, 7> to_world{q.w(), q.x(), q.y(), q.z(), t.x(), t.y(), t.z()};
+                if (!cloud->extract_points(depth, cv::cuda::PtrStepb(), to_world, 0))
+                    throw cuphoto::CuPhotoException("extract_points failed");
+                const std::string ply = arg(argc, argv, "--points_ply", "");
+                if (!ply.empty() && !cloud->save_ply(ply)) throw cuphoto::CuPhotoException("save_ply failed");
+                std::printf("points %llu\n", (unsigned long long)cloud->get_num_points());
+                tsdf.reconstruct_surface(cloud);
+            } else {
+                tsdf.reconstruct_surface(rgb, depth);
+            }
         } else {
             const int n = std::atoi(arg(argc, argv, "--frames", "1").c_str());
             const int per_pass = std::atoi(arg(argc, argv, "--per_pass", "16").c_str());

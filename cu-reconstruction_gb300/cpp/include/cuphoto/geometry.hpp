@@ -99,6 +99,14 @@ public:
     Mat3 rotationMatrix() const { return q_.matrix(); }
     Vec3 translation() const { return t_; }
     Quat unit_quaternion() const { return q_; }
+    // The inverse transform (Sophus::SE3d::inverse): R^T, -R^T t.
+    SE3 inverse() const {
+        const Quat qi(q_.qw, -q_.qx, -q_.qy, -q_.qz);
+        const Mat3 Ri = qi.matrix();
+        Vec3 ti;
+        for (int r = 0; r < 3; ++r) ti(r) = -(Ri(r, 0) * t_(0) + Ri(r, 1) * t_(1) + Ri(r, 2) * t_(2));
+        return SE3(qi, ti);
+    }
 
 private:
     Quat q_;

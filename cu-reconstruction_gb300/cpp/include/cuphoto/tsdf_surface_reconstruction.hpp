@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "config.hpp"
+#include "cuda_point_cloud.cuh"
 #include "cv_types.hpp"
 #include "geometry.hpp"
 #include "mesh.hpp"
@@ -36,6 +37,13 @@ public:
     TSDFSurface(const Config& cfg);
 
     void reconstruct_surface(const cv::cuda::GpuMat& color, const cv::cuda::GpuMat& depth);
+
+    // The cloud projected to colour + depth at the configured pose
+    // (project_to_color_depth), then integrated and meshed.  The reference's
+    // version (tsdf_surface_reconstruction.cpp:94-120) stops after the
+    // projection, with its integrate and mesh calls commented out, and first
+    // estimates normals with PCL, which nothing reads; both are left out here.
+    void reconstruct_surface(const cudaPointCloud::Ptr cuda_pc);
 
     // frames: device depth images; poses: world-to-camera {qw,qx,qy,qz,tx,ty,tz}
     void reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass = 16);

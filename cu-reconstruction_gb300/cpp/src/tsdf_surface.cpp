@@ -96,6 +96,15 @@ void TSDFSurface::reconstruct_surface(const cv::cuda::GpuMat& color, const cv::c
     mesh_from(tsdf_volume);
 }
 
+void TSDFSurface::reconstruct_surface(const cudaPointCloud::Ptr cuda_pc) {
+    cv::cuda::GpuMat gpu_depth((int)camera_height, (int)camera_width, CV_32F);
+    cv::cuda::GpuMat gpu_color((int)camera_height, (int)camera_width, CV_8UC3);
+    if (!cuda_pc->project_to_color_depth(gpu_color, gpu_depth, global_pose())) return;
+    TSDFVolume tsdf_volume(build_cfg(), engine_options);
+    tsdf_volume.integrate(gpu_color, gpu_depth, global_pose());
+    mesh_from(tsdf_volume);
+}
+
 void TSDFSurface::reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass) {
     TSDFVolume tsdf_volume(build_cfg(), engine_options);
     if (frames_per_pass < 1) frames_per_pass = 1;

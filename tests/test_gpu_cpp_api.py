@@ -153,3 +153,39 @@ def test_headless_example_reports_missing_config(engine_lib, tmp_path):
                        timeout=60)
     assert r.returncode == 1
     assert "does not exist" in r.stderr
+
+
+@pytest.mark.gpu
+def test_headless_point_cloud_path(gpu, tmp_path):
+    """reconstruct_surface(cudaPointCloud) through the C++ layer: the frame is
+    back-projected into a cloud at the inverse of the configured pose, stored
+    with save_ply, projected back and integrated.  The depth image it gets
+    back is the frame up to pixels whose round trip truncates to a neighbour
+    (the reference's pixel rule), which leaves holes, so its mesh is a large
+    part of the depth-image path's; both in the fixed mode.  Each step's
+    arithmetic is checked bit for bit in test_gpu_points."""
+    cam = S.Camera.half()
+    seq = S.make_sequence(1, scene_id=3, camera=cam, trajectory="frontal")
+    grid, phys, off = (96, 80, 64), (1.6, 1.2, 1.28), (-0.8, -0.6, 0.3)
+    (tmp_path / "depth.u16").write_bytes(seq.depth_u16[0].astype("<u2").tobytes())
+    extra = ("tsdf.engine.mode: fixed\ntsdf.volume.camera.pose.euler.yaw: 4.0\n"
+             "tsdf.volume.camera.pose.translation.x: 0.03\n")
+    counts = {}
+    for mode in ("depth", "points"):
+        ply = str(tmp_path / ("%s.ply" % mode))
+        cfgp = str(tmp_path / ("%s.yaml" % mode))
+        write_config(cfgp, grid, phys, off, cam, ply, extra)
+        cmd = [EXAMPLE, "--config_path", cfgp, "--depth", str(tmp_path / "depth.u16")]
+        if mode == "points":
+            cmd += ["--points", "--points_ply", str(tmp_path / "cloud.ply")]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+        V, F = read_ply(ply)
+        counts[mode] = len(F)
+        if mode == "points":
+            assert "points %d" % (cam.width * cam.height) in r.stdout
+    lines = (tmp_path / "cloud.ply").read_text().splitlines()
+    assert lines[:3] == ["ply", "format ascii 1.0", "element vertex %d" % (cam.width * cam.height)]
+    assert lines[9] == "end_header" and len(lines) == 10 + cam.width * cam.height
+    assert counts["depth"] > 300, counts
+    assert 0.5 * counts["depth"] <= counts["points"] <= 1.1 * counts["depth"], counts
