@@ -48,10 +48,11 @@ def parse():
     ap.add_argument("--refine-lr", type=float, default=3e-4)
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff", "refine"],
+    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff", "refine", "points"],
                     help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames; "
                          "diff: forward + adjoint timing and finite-difference check at 128^3 x 16 frames; "
-                         "refine: 1024^3 x 1000 frames 1280x720, then pose refinement of 64 jittered frames")
+                         "refine: 1024^3 x 1000 frames 1280x720, then pose refinement of 64 jittered frames; "
+                         "points: 30 frames 640x480 to a cloud, projected to a view")
     a = ap.parse_args()
     if a.grid is None:
         a.grid = 1024 if a.workload == "refine" else 512
@@ -563,6 +564,93 @@ def refine_workload(args, torch):
             "reduction": {k: 1 - after[k] / before[k] for k in before}}
 
 
+def points_workload(args, torch, nframes=30, reps=5):
+    """Point clouds: 30 ray-cast 640x480 frames around a plane + 6 spheres
+    back-projected into one 9.2 M-point cloud (gbt_points_extract, CUDA
+    events per frame), then the cloud projected to colour + depth at another
+    pose (gbt_points_project: 64-bit atomic-min z-buffer + resolve).  Beside
+    them: the reference's own point_cloud_extract kernel launched as
+    extract_points launches it (one launch + sync per frame), and its
+    project_to_color_depth host loop restated single-threaded (the oracle)
+    on the same cloud, whose images the engine must match bit for bit."""
+    import ctypes as C
+    import oracle
+    from cuphoto import _lib as L
+    from cuphoto import synthetic as S
+    cam = S.Camera()
+    W, H = cam.width, cam.height
+    K = [cam.fx, 0, cam.cx, 0, cam.fy, cam.cy, cam.cx, cam.cy, 1.0]   # both readings agree
+    scene = S.make_scene(0)
+    poses = S.circle_poses(nframes)
+    raw = S.render_sequence_torch(scene, poses, cam, seed=0)
+    depth = (raw.to(torch.int32) & 0xFFFF).to(torch.float32) * np.float32(0.001)
+    inv = []
+    for p in poses:
+        R = S.matrix_from_quat(p[:4])
+        inv.append(S.pose7(R.T, -R.T @ p[4:]))
+    n = nframes * W * H
+    cloud = torch.zeros((n, 33), dtype=torch.uint8, device="cuda")
+    lib = L.lib()
+    Kc = (C.c_double * 9)(*K)
+
+    def extract(k):
+        L.check(lib.gbt_points_extract(C.byref(Kc), C.c_void_p(depth[k].data_ptr()), W * 4, L.DEPTH_F32_M, 1.0, None,
+                                       0, W, H, C.byref((C.c_double * 7)(*inv[k])), k * W * H,
+                                       C.c_void_p(cloud.data_ptr()), n, None))
+
+    for k in range(nframes):
+        extract(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        for k in range(nframes):
+            extract(k)
+    e1.record()
+    torch.cuda.synchronize()
+    ext_ms = e0.elapsed_time(e1) / reps
+    view = S.circle_poses(nframes * 2)[1]
+    dimg = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    cimg = torch.zeros((H, W, 3), dtype=torch.uint8, device="cuda")
+    scratch = torch.empty(W * H, dtype=torch.int64, device="cuda")
+    Vp = (C.c_double * 7)(*view)
+
+    def project():
+        L.check(lib.gbt_points_project(C.c_void_p(cloud.data_ptr()), n, C.byref(Kc), C.byref(Vp),
+                                       C.c_void_p(dimg.data_ptr()), W * 4, C.c_void_p(cimg.data_ptr()), W * 3, W, H,
+                                       C.c_void_p(scratch.data_ptr()), None))
+
+    project()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        project()
+    e1.record()
+    torch.cuda.synchronize()
+    proj_ms = e0.elapsed_time(e1) / reps
+    out = {"workload": "points: %d frames %dx%d -> %d points, projected to a %dx%d view" % (nframes, W, H, n, W, H),
+           "extract": {"ms_per_frame": ext_ms / nframes, "points_per_s": n / (ext_ms * 1e-3)},
+           "project": {"ms": proj_ms, "points_per_s": n / (proj_ms * 1e-3), "pixels_hit": int((dimg > 0).sum())}}
+    host = cloud.cpu().numpy()
+    t0 = time.perf_counter()
+    ed, ec = oracle.points_project(host, K, view, W, H)
+    cpu_s = time.perf_counter() - t0
+    out["reference_host_loop"] = {"kind": "port", "cores": 1, "s": cpu_s, "points_per_s": n / cpu_s,
+                                  "what": "project_to_color_depth's host z-buffer loop, restated (the oracle)"}
+    out["parity_with_host_loop"] = bool(np.array_equal(dimg.cpu().numpy().view(np.uint32), ed.view(np.uint32))
+                                        and np.array_equal(cimg.cpu().numpy(), ec))
+    if oracle.RefHarness.available():
+        ref = torch.full_like(cloud[: W * H], 0)
+        oracle.RefHarness.lib()
+        t0 = time.perf_counter()
+        for k in range(nframes):
+            oracle.RefHarness.points_extract(K, depth[k].data_ptr(), W * 4, W, H, 0, 0, inv[k], 0, ref.data_ptr())
+        wall = time.perf_counter() - t0
+        out["reference_extract"] = {"ms_per_frame": 1e3 * wall / nframes, "points_per_s": n / wall,
+                                    "what": "point_cloud_extract of the reference, one launch + sync per frame"}
+    return out
+
+
 def run_reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -775,6 +863,15 @@ def main():
         spec.loader.exec_module(eb)
         eb.build()
         print(json.dumps(refine_workload(args, torch)), flush=True)
+        return
+    if args.workload == "points":
+        import torch
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+        eb = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(eb)
+        eb.build()
+        print(json.dumps(points_workload(args, torch)), flush=True)
         return
     if args.workload == "diff":
         import torch
