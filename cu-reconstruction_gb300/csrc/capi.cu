@@ -54,6 +54,9 @@ struct gbt_volume {
     // marching-cubes scratch: [0,64) header (ticket u32, error i32, total i64), then status words
     void* mc_scratch;
     size_t mc_scratch_bytes;
+    // shared-vertex mesh scratch: used-edge bits, word offsets, block sums, vertex count
+    void* weld_scratch;
+    size_t weld_scratch_bytes;
 };
 
 namespace gbt {
@@ -226,6 +229,7 @@ gbt_status gbt_volume_destroy(gbt_volume* v) {
     cudaFree(v->desc.W);
     if (v->tvox) cudaFree(v->tvox);
     if (v->mc_scratch) cudaFree(v->mc_scratch);
+    if (v->weld_scratch) cudaFree(v->weld_scratch);
     delete v;
     return GBT_OK;
 }
@@ -331,10 +335,11 @@ gbt_status gbt_integrate(gbt_volume* v, const gbt_frame* frames, int32_t nframes
 
 namespace {
 
-gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, int64_t index_base, gbt::McArgs* a) {
+gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, int64_t index_base, gbt::McArgs* a,
+                      bool indexed = false) {
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     if (cap < 0) return fail(GBT_ERR_INVALID_ARG, "negative capacity");
-    if (cap > 0 && (!verts || !tris)) return fail(GBT_ERR_INVALID_ARG, "output buffers are NULL");
+    if (cap > 0 && ((!verts && !indexed) || !tris)) return fail(GBT_ERR_INVALID_ARG, "output buffers are NULL");
     const gbt::VolDesc& d = v->desc;
     std::memset(a, 0, sizeof(*a));
     a->D = d.D;
@@ -721,6 +726,85 @@ gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, con
     cudaGetLastError();
     cudaError_t e = gbt::launch_diff_backward(a, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "differentiable backward");
+    return GBT_OK;
+}
+
+gbt_status gbt_extract_mesh_indexed(gbt_volume* v, float* verts, float* normals, int32_t* tris, int64_t cap_verts,
+                                    int64_t cap_tris, int64_t index_base, int64_t* n_verts, int64_t* n_tris,
+                                    void* stream) {
+    if (!n_verts || !n_tris) return fail(GBT_ERR_INVALID_ARG, "gbt_extract_mesh_indexed: n_verts or n_tris is NULL");
+    *n_verts = 0;
+    *n_tris = 0;
+    if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    if (v->cfg.mode != GBT_MODE_FIXED)
+        return fail(GBT_ERR_INVALID_ARG,
+                    "gbt_extract_mesh_indexed: fixed mode only (compat emits three vertices per triangle, as the "
+                    "reference does)");
+    if (cap_verts < 0 || (cap_verts > 0 && !verts)) return fail(GBT_ERR_INVALID_ARG, "vertex buffer is NULL");
+    gbt::McArgs a;
+    gbt_status st = mc_prepare(v, nullptr, tris, cap_tris, index_base, &a, true);
+    if (st != GBT_OK) return st;
+    const gbt::VolDesc& d = v->desc;
+    gbt::WeldArgs w;
+    std::memset(&w, 0, sizeof(w));
+    w.nwords = (3 * v->nvox + 31) / 32;
+    w.nblocks = (w.nwords + gbt::kWeldWordsPerBlock - 1) / gbt::kWeldWordsPerBlock;
+    const size_t need = 64 + (size_t)w.nwords * 8 + (size_t)w.nblocks * 4;
+    if (v->weld_scratch_bytes < need) {
+        if (v->weld_scratch) cudaFree(v->weld_scratch);
+        v->weld_scratch = nullptr;
+        v->weld_scratch_bytes = 0;
+        cudaError_t e = cudaMalloc(&v->weld_scratch, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GBT_ERR_ALLOC, "allocating %zu bytes of vertex-sharing scratch: %s", need, cudaGetErrorString(e));
+        }
+        v->weld_scratch_bytes = need;
+    }
+    char* sp = static_cast<char*>(v->weld_scratch);
+    w.nverts = reinterpret_cast<long long*>(sp);
+    w.bits = reinterpret_cast<uint32_t*>(sp + 64);
+    w.word_offset = w.bits + w.nwords;
+    w.block_sums = w.word_offset + w.nwords;
+    (void)d;
+    cudaStream_t s = as_stream(stream);
+    cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(w.bits, 0, (size_t)w.nwords * 4, s);
+    if (e != cudaSuccess) return cuda_fail(e, "vertex-sharing scratch clear");
+    w.mc = a;
+    e = gbt::launch_weld_fixed(w, s);
+    if (e != cudaSuccess) return cuda_fail(e, "edge marking");
+    long long nv = 0;
+    e = cudaMemcpyAsync(&nv, w.nverts, sizeof(nv), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "vertex count");
+    if (nv > (long long)INT32_MAX - (index_base > 0 ? index_base : 0))
+        return fail(GBT_ERR_INVALID_ARG, "%lld vertices do not fit 32-bit triangle indices", nv);
+    *n_verts = nv;
+    if (verts && cap_verts > 0) {
+        w.verts = verts;
+        w.normals = normals;
+        w.cap_verts = cap_verts;
+        e = gbt::launch_weld_vertices_fixed(w, s);
+        if (e != cudaSuccess) return cuda_fail(e, "vertices");
+    }
+    a.edge_bits = w.bits;
+    a.edge_word_offset = w.word_offset;
+    st = mc_launch(v, a, s);
+    if (st != GBT_OK) return st;
+    struct {
+        unsigned int ticket;
+        int error;
+        long long total;
+    } hdr;
+    e = cudaMemcpyAsync(&hdr, v->mc_scratch, sizeof(hdr), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh extraction");
+    if (hdr.error) return fail(GBT_ERR_TIMEOUT, "mesh extraction: a tile gave up waiting for its predecessor");
+    *n_tris = hdr.total;
+    if ((hdr.total > cap_tris && cap_tris > 0) || (nv > cap_verts && cap_verts > 0))
+        return fail(GBT_ERR_CAPACITY, "mesh has %lld vertices and %lld triangles, buffers hold %lld and %lld", nv,
+                    hdr.total, (long long)cap_verts, (long long)cap_tris);
     return GBT_OK;
 }
 

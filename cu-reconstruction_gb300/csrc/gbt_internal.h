@@ -116,7 +116,28 @@ struct McArgs {
     unsigned int* ticket;        // tile ticket, zeroed before launch
     long long* total;            // triangle count out
     int* error;                  // set to 1 when a look-back wait gives up
+    // Fixed mode with shared vertices: when edge_bits is set, triangles are
+    // written as indices of the vertices of their grid edges (edge
+    // 3 * voxel + axis; vertex index = edge_word_offset[edge / 32] + the set
+    // bits of edge_bits below it) and verts is not written.
+    const uint32_t* edge_bits;
+    const uint32_t* edge_word_offset;
 };
+
+// Fixed-mode mesh with shared vertices (k_ieee.cu): the edges used by the
+// triangles, their vertex numbering and the vertices with normals.
+struct WeldArgs {
+    McArgs mc;
+    uint32_t* bits;          // [nwords] used-edge bitmask
+    uint32_t* word_offset;   // [nwords] vertex index of each word's first used edge
+    uint32_t* block_sums;    // [nblocks] used edges per block of kWeldWordsPerBlock words
+    long long* nverts;       // total out
+    int64_t nwords, nblocks;
+    float* verts;            // 3 per vertex
+    float* normals;          // 3 per vertex, or NULL
+    int64_t cap_verts;
+};
+constexpr int kWeldWordsPerBlock = 1024;
 
 // Differentiable integrate (k_diff.cu).  dtype 0: float, 1: double for the
 // volume, depth, rotations and translations; gradients of depth and pose are
@@ -151,6 +172,8 @@ cudaError_t launch_integrate_compat_ieee(const IntegrateArgs& a, int brick, int 
 cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, cudaStream_t s);
 cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s);
 cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s);
+cudaError_t launch_weld_fixed(const WeldArgs& a, cudaStream_t s);         // marks edges, numbers vertices
+cudaError_t launch_weld_vertices_fixed(const WeldArgs& a, cudaStream_t s);
 // Batched integrate (one persistent launch over many volumes).
 cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s);

@@ -559,6 +559,15 @@ __device__ __forceinline__ int64_t corner_index(const McArgs& a, int64_t b0, int
     return (corner_dz(k) ? b1 : b0) + corner_dx(k) + (corner_dy(k) ? a.gx : 0);
 }
 
+// Grid edge of cube (cx, cy, cz) between corners ca (the lower one) and cb:
+// 3 * (linear index of ca's voxel) + the axis along which they differ.
+__device__ __forceinline__ int64_t weld_edge_id(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int ca, int cb) {
+    const int axis = corner_dx(ca) != corner_dx(cb) ? 0 : (corner_dy(ca) != corner_dy(cb) ? 1 : 2);
+    const int64_t lin = ((int64_t)(cz + corner_dz(ca)) * a.gy + (int64_t)(cy + corner_dy(ca))) * a.gx +
+                        (int64_t)(cx + corner_dx(ca));
+    return 3 * lin + axis;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McArgs a) {
     __shared__ unsigned char s_count[256];
@@ -732,6 +741,13 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
                             const int tc = ca; ca = cb; cb = tc;
                             const float ts = sa; sa = sb; sb = ts;
                         }
+                        if (a.edge_bits) {   // shared vertices: the index of this edge's vertex
+                            const int64_t id = weld_edge_id(a, cx, cy, cz, ca, cb);
+                            const uint32_t word = a.edge_bits[id >> 5];
+                            const uint32_t below = word & ((1u << (id & 31)) - 1u);
+                            a.tris[3 * out + j] = (int32_t)(a.index_base + a.edge_word_offset[id >> 5] + __popc(below));
+                            continue;
+                        }
                         pa[0] = centre((int)cx + corner_dx(ca), a.vs[0], a.off[0]);
                         pa[1] = centre((int)cy + corner_dy(ca), a.vs[1], a.off[1]);
                         pa[2] = centre((int)cz + corner_dz(ca), a.vs[2], a.off[2]);
@@ -749,6 +765,204 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
         }
     }
 }
+
+#if !defined(GBT_REF_ARITH)
+// ---------------------------------------------------------------------------
+// Fixed-mode mesh with shared vertices.  (1) weld_mark: every cube that the
+// fixed-mode marching cubes emits sets the bits of the grid edges its
+// triangles use; (2) weld_count / weld_scan_blocks / weld_offsets: an
+// exclusive scan of the bit counts numbers the used edges (vertex index =
+// word offset + set bits below); (3) weld_vertices: one vertex per used
+// edge, interpolated exactly as mc_kernel<kFixed> interpolates it (lower
+// endpoint first, so the positions are the ones the triangle soup holds),
+// with the normal of the interpolated central-difference gradient;
+// (4) mc_kernel<kFixed> with edge_bits set writes the triangles as indices,
+// in the same order as the triangle soup.
+__global__ void __launch_bounds__(256) weld_mark_kernel(const __grid_constant__ McArgs a, uint32_t* bits) {
+    __shared__ unsigned char s_count[256];
+    __shared__ unsigned long long s_tri[256];
+    __shared__ unsigned char s_ends[12];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+        s_count[k] = GBT_MC_TRI_COUNT[k];
+        s_tri[k] = GBT_MC_TRI_PACKED[k];
+    }
+    if (threadIdx.x < 12) s_ends[threadIdx.x] = GBT_MC_EDGE_ENDS[threadIdx.x];
+    __syncthreads();
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncubes; c += gridDim.x * blockDim.x) {
+        const uint32_t row = fastdiv(c, a.div_cx);
+        const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
+        const uint32_t cz = fastdiv(row, a.div_cy);
+        const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+        int64_t b0, b1;
+        cube_base<kFixed>(a, cx, cy, cz, &b0, &b1);
+        int t = 0;
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int64_t idx = corner_index<kFixed>(a, b0, b1, k);
+            ok = ok && (__ldg(a.W + idx) > 0.f);
+            if (__ldg(a.D + idx) < 0.f) t |= 1 << k;
+        }
+        if (!ok) continue;
+        const int n = s_count[t];
+        const unsigned long long edges = s_tri[t];
+        for (int q = 0; q < 3 * n; ++q) {
+            const int e = (int)((edges >> (4 * q)) & 15ull);
+            int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
+            if (corner_dx(ca) + corner_dy(ca) + corner_dz(ca) > corner_dx(cb) + corner_dy(cb) + corner_dz(cb)) {
+                const int tc = ca; ca = cb; cb = tc;
+            }
+            const int64_t id = weld_edge_id(a, cx, cy, cz, ca, cb);
+            atomicOr(bits + (id >> 5), 1u << (id & 31));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_warp) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += s_warp[w];
+    return t;
+}
+
+// used edges per block of kWeldWordsPerBlock words (256 threads x 4 words)
+__global__ void __launch_bounds__(256) weld_count_kernel(const uint32_t* bits, int64_t nwords, uint32_t* block_sums) {
+    __shared__ uint32_t s_warp[8];
+    const int64_t base = (int64_t)blockIdx.x * kWeldWordsPerBlock + 4 * threadIdx.x;
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k < nwords) v += __popc(bits[base + k]);
+    const uint32_t t = block_sum_256(v, s_warp);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = t;
+}
+
+// exclusive scan of the block sums in place, one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) weld_scan_blocks_kernel(uint32_t* block_sums, int64_t nblocks,
+                                                                long long* nverts) {
+    __shared__ unsigned long long s_part[32];
+    __shared__ unsigned long long s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t base = 0; base < nblocks; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const unsigned long long v = i < nblocks ? block_sums[i] : 0ull;
+        unsigned long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_part[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long p = s_part[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, p, o);
+                if (lane >= o) p += y;
+            }
+            s_part[lane] = p;
+        }
+        __syncthreads();
+        const unsigned long long before = s_carry + (warp ? s_part[warp - 1] : 0ull) + x - v;
+        if (i < nblocks) block_sums[i] = (uint32_t)before;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_part[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *nverts = (long long)s_carry;
+}
+
+// vertex index of each word's first used edge
+__global__ void __launch_bounds__(256) weld_offsets_kernel(const uint32_t* bits, int64_t nwords,
+                                                           const uint32_t* block_offsets, uint32_t* word_offset) {
+    __shared__ uint32_t s_warp[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kWeldWordsPerBlock + 4 * threadIdx.x;
+    uint32_t c[4];
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        c[k] = base + k < nwords ? (uint32_t)__popc(bits[base + k]) : 0u;
+        v += c[k];
+    }
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t before = block_offsets[blockIdx.x] + x - v;
+    for (int w = 0; w < warp; ++w) before += s_warp[w];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < nwords) word_offset[base + k] = before;
+        before += c[k];
+    }
+}
+
+__device__ __forceinline__ void weld_gradient(const McArgs& a, int x, int y, int z, float* g) {
+    const int n[3] = {a.gx, a.gy, a.gz};
+    const int p[3] = {x, y, z};
+    const int64_t stride[3] = {1, (int64_t)a.gx, (int64_t)a.gx * a.gy};
+    const int64_t i = (int64_t)z * stride[2] + (int64_t)y * stride[1] + x;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int lo = p[q] > 0 ? 1 : 0, hi = p[q] + 1 < n[q] ? 1 : 0;
+        const float d0 = a.D[i - lo * stride[q]], d1 = a.D[i + hi * stride[q]];
+        g[q] = (lo + hi) ? (d1 - d0) / ((float)(lo + hi) * a.vs[q]) : 0.f;
+    }
+}
+
+__global__ void __launch_bounds__(256) weld_vertices_kernel(const __grid_constant__ WeldArgs w) {
+    const McArgs& a = w.mc;
+    for (int64_t word = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; word < w.nwords;
+         word += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t m = w.bits[word];
+        int64_t vid = w.word_offset[word];
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const int64_t id = word * 32 + k;
+            const int64_t lin = id / 3;
+            const int axis = (int)(id - 3 * lin);
+            const uint32_t row = fastdiv((uint32_t)lin, a.div_gx);
+            const int x = (int)((uint32_t)lin - row * (uint32_t)a.gx);
+            const uint32_t zz = fastdiv(row, a.div_gy);
+            const int y = (int)(row - zz * (uint32_t)a.gy), z = (int)zz;
+            const int x1 = x + (axis == 0), y1 = y + (axis == 1), z1 = z + (axis == 2);
+            const int64_t lin1 = ((int64_t)z1 * a.gy + y1) * a.gx + x1;
+            const float sa = a.D[lin], sb = a.D[lin1];
+            const float pa[3] = {centre(x, a.vs[0], a.off[0]), centre(y, a.vs[1], a.off[1]), centre(z, a.vs[2], a.off[2])};
+            const float pb[3] = {centre(x1, a.vs[0], a.off[0]), centre(y1, a.vs[1], a.off[1]),
+                                 centre(z1, a.vs[2], a.off[2])};
+            const float r = __fdiv_rn(sa, __fsub_rn(sa, sb));
+            if (vid < w.cap_verts) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) w.verts[3 * vid + q] = __fmaf_rn(r, __fsub_rn(pb[q], pa[q]), pa[q]);
+                if (w.normals) {
+                    float ga[3], gb[3], nrm[3];
+                    weld_gradient(a, x, y, z, ga);
+                    weld_gradient(a, x1, y1, z1, gb);
+                    float ss = 0.f;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        nrm[q] = ga[q] + r * (gb[q] - ga[q]);
+                        ss += nrm[q] * nrm[q];
+                    }
+                    const float inv = ss > 0.f ? rsqrtf(ss) : 0.f;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) w.normals[3 * vid + q] = nrm[q] * inv;
+                }
+            }
+            ++vid;
+        }
+    }
+}
+#endif
 
 // ---------------------------------------------------------------------------
 template <int MODE, int TX, int BY, int BZ>

@@ -28,4 +28,32 @@ cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s) { return laun
 
 cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kFixed>(a, s); }
 
+namespace {
+unsigned weld_grid(int64_t n) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
+    }
+    const int64_t want = (n + 255) / 256;
+    const int64_t cap = (int64_t)sms * 16;
+    return (unsigned)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+}  // namespace
+
+cudaError_t launch_weld_fixed(const WeldArgs& w, cudaStream_t s) {
+    ieeearith::weld_mark_kernel<<<weld_grid(w.mc.ncubes), 256, 0, s>>>(w.mc, w.bits);
+    ieeearith::weld_count_kernel<<<(unsigned)w.nblocks, 256, 0, s>>>(w.bits, w.nwords, w.block_sums);
+    ieeearith::weld_scan_blocks_kernel<<<1, 1024, 0, s>>>(w.block_sums, w.nblocks, w.nverts);
+    ieeearith::weld_offsets_kernel<<<(unsigned)w.nblocks, 256, 0, s>>>(w.bits, w.nwords, w.block_sums, w.word_offset);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weld_vertices_fixed(const WeldArgs& w, cudaStream_t s) {
+    ieeearith::weld_vertices_kernel<<<weld_grid(w.nwords), 256, 0, s>>>(w);
+    return cudaGetLastError();
+}
+
 }  // namespace gbt

@@ -115,6 +115,8 @@ SIGNATURES = [
                                    C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                          C.c_void_p, C.c_void_p]),
+    ("gbt_extract_mesh_indexed", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
+                                           C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
     ("gbt_extract_mesh_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64,
                                            C.c_void_p, C.c_void_p]),
     ("gbt_points_extract", C.c_int, [C.POINTER(C.c_double * 9), C.c_void_p, C.c_int64, C.c_int32, C.c_float,

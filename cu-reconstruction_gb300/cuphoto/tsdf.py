@@ -220,6 +220,24 @@ class TSDFVolume:
                                   depth_scale=depth_scale, stream=stream, **kw)
 
 
+def extract_mesh_indexed(volume, normals=True, index_base=0, stream=None):
+    """Fixed-mode mesh with shared vertices (gbt_extract_mesh_indexed):
+    (verts (V, 3) f32, normals (V, 3) f32 or None, tris (T, 3) i32) CUDA
+    tensors; the triangles are extract_mesh_device's, in the same order."""
+    torch = _torch()
+    lib = L.lib()
+    s = _stream_handle(stream)
+    nv, nt = C.c_int64(), C.c_int64()
+    L.check(lib.gbt_extract_mesh_indexed(volume.handle, None, None, None, 0, 0, index_base, C.byref(nv), C.byref(nt), s))
+    V = torch.empty((max(nv.value, 1), 3), dtype=torch.float32, device="cuda")
+    N = torch.empty((max(nv.value, 1), 3), dtype=torch.float32, device="cuda") if normals else None
+    T = torch.empty((max(nt.value, 1), 3), dtype=torch.int32, device="cuda")
+    L.check(lib.gbt_extract_mesh_indexed(volume.handle, C.c_void_p(V.data_ptr()),
+                                         C.c_void_p(N.data_ptr()) if normals else None, C.c_void_p(T.data_ptr()),
+                                         nv.value, nt.value, index_base, C.byref(nv), C.byref(nt), s))
+    return V[:nv.value], (N[:nv.value] if normals else None), T[:nt.value]
+
+
 def extract_mesh_device(volume, capacity=None, index_base=0, stream=None):
     """Runs the engine's marching cubes; returns (verts (T,3,3) f32, tris (T,3) i32) CUDA tensors."""
     torch = _torch()

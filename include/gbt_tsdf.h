@@ -253,6 +253,21 @@ gbt_status gbt_extract_mesh(gbt_volume* vol, float* verts, int32_t* tris, int64_
 gbt_status gbt_extract_mesh_async(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                   int64_t index_base, int64_t* d_n_tris, void* stream);
 
+/* Fixed-mode mesh with shared vertices and normals.  No counterpart in the
+ * reference (its mesh has three vertices per triangle, which the compat mode
+ * keeps).  The triangles are those of gbt_extract_mesh, in the same order;
+ * each grid edge crossed by the surface gives one vertex, at the position
+ * gbt_extract_mesh writes for it (bit for bit), and tris holds 3 vertex
+ * indices per triangle (index_base + vertex).  normals (NULL: none) gets the
+ * unit normal of the interpolated central-difference gradient of the
+ * distances, pointing to free space.  Synchronises `stream`; counts are
+ * returned in *n_verts, *n_tris; GBT_ERR_CAPACITY if either exceeds its
+ * buffer (outputs then partial); verts/tris may be NULL with capacity 0
+ * (counts only).  Fixed-mode volumes only. */
+gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normals, int32_t* tris, int64_t cap_verts,
+                                    int64_t cap_tris, int64_t index_base, int64_t* n_verts, int64_t* n_tris,
+                                    void* stream);
+
 /* Mesh extraction for callers that cannot allocate device memory.
  *
  * No counterpart in the reference: it is an engine addition.  It is meant for

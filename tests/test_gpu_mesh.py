@@ -164,3 +164,78 @@ def test_large_field_mesh_tiles_chain(gpu, oracle):
     Vo, To = oracle.mc_fixed(oracle.cfg_from(tc), D.ravel(), W.ravel())
     assert len(V) == len(Vo) > 10000
     assert np.array_equal(V.view(np.uint32), Vo.view(np.uint32))
+
+
+# ---------------------------------------------------------------------------
+# Fixed-mode mesh with shared vertices (gbt_extract_mesh_indexed)
+def _scene_normals(scene, P):
+    """Unit gradient of the scene's analytic SDF (plane + spheres) at P (n, 3)."""
+    P = np.asarray(P, np.float64)
+    d = scene.plane_up * (P[:, 1] - scene.plane_y)
+    g = np.tile([0.0, scene.plane_up, 0.0], (len(P), 1))
+    for c, r in zip(scene.centres, scene.radii):
+        v = P - c
+        n = np.linalg.norm(v, axis=1)
+        ds = n - r
+        nearer = ds < d
+        d = np.where(nearer, ds, d)
+        g = np.where(nearer[:, None], v / np.maximum(n, 1e-12)[:, None], g)
+    return g
+
+
+@pytest.mark.parametrize("grid", [(64, 48, 40), (33, 65, 17)])
+def test_indexed_mesh_is_the_soup_with_shared_vertices(gpu, grid):
+    """The shared-vertex mesh gathers back to the triangle soup bit for bit,
+    in the same triangle order; every vertex is used and none repeats."""
+    from cuphoto import extract_mesh_indexed
+    tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=tuple(0.01 * g for g in grid),
+                          global_offset=(-0.3, 0.2, 0.5), mode="fixed", max_weight=16)
+    vol = TSDFVolume(tc)
+    D = smooth_field(grid[::-1], 7 + sum(grid))
+    W = (np.random.default_rng(1).random(D.shape) > 0.02).astype(np.float32)
+    set_distances(gpu, vol, D, W)
+    V, T = mesh(vol)
+    Vi, Ni, Ti = (x.cpu().numpy() for x in extract_mesh_indexed(vol))
+    assert len(Ti) == len(T) > 100
+    assert np.array_equal(Vi[Ti].view(np.uint32), V.view(np.uint32))
+    assert np.unique(Ti).size == len(Vi)                 # no orphan vertices
+    assert len(Vi) < 0.6 * 3 * len(Ti)                   # each vertex shared by several triangles
+    assert len(np.unique(Vi, axis=0)) >= 0.999 * len(Vi)
+    n = np.linalg.norm(Ni, axis=1)
+    assert np.all(np.abs(n - 1) < 1e-5)
+
+
+def test_indexed_mesh_normals_point_to_free_space(gpu):
+    """On an integrated scene the normals agree with the analytic surface
+    normals, and the triangle winding is consistent with them."""
+    from cuphoto import extract_mesh_indexed
+    seq, tc = circle_case(n=96, frames=8, mode="fixed")
+    vol, _, _ = engine_run(gpu, tc, seq.depth_u16, seq.poses, k=8)
+    Vi, Ni, Ti = (x.cpu().numpy() for x in extract_mesh_indexed(vol))
+    assert len(Ti) > 1000
+    g = _scene_normals(seq.scene, Vi)
+    assert (np.sum(Ni * g, axis=1) > 0.7).mean() > 0.9
+    tri = Vi[Ti]
+    face = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    s = np.sign(np.sum(face * Ni[Ti].mean(axis=1), axis=1))
+    assert max((s > 0).mean(), (s < 0).mean()) > 0.95
+
+
+def test_indexed_mesh_capacity_counts_and_mode(gpu):
+    from cuphoto import extract_mesh_indexed
+    grid = (40, 36, 32)
+    tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=(0.4, 0.36, 0.32), mode="fixed")
+    vol = TSDFVolume(tc)
+    D = smooth_field(grid[::-1], 3)
+    set_distances(gpu, vol, D, np.ones_like(D))
+    Vi, _, Ti = extract_mesh_indexed(vol, normals=False)
+    lib = L.lib()
+    nv, nt = C.c_int64(), C.c_int64()
+    small = gpu.empty((10, 3), dtype=gpu.float32, device="cuda")
+    tris = gpu.empty((len(Ti), 3), dtype=gpu.int32, device="cuda")
+    st = lib.gbt_extract_mesh_indexed(vol.handle, C.c_void_p(small.data_ptr()), None, C.c_void_p(tris.data_ptr()),
+                                      10, len(Ti), 0, C.byref(nv), C.byref(nt), None)
+    assert st == L.GBT_ERR_CAPACITY and nv.value == len(Vi) and nt.value == len(Ti)
+    compat = TSDFVolume(TSDFVolumeConfig(voxel_grid_size=grid, physical_size=(0.4, 0.36, 0.32)))
+    with pytest.raises(L.GbtError):
+        extract_mesh_indexed(compat)
