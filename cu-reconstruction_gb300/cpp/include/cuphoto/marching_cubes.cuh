@@ -16,6 +16,14 @@ namespace cuphoto {
 void generate_triangular_surface(const TSDFVolume& tsdf_volume, std::vector<float3>& verts,
                                  std::vector<int3>& triangles);
 
+// Engine addition for fixed-mode volumes (gbt_extract_mesh_indexed): the same
+// triangles with one vertex per crossed grid edge and per-vertex normals.
+// Appends like generate_triangular_surface (indices offset by the vertices
+// already in `verts`; `normals` is kept the same length as `verts`).
+// Returns false, after logging, on a compat volume or a failure.
+bool generate_indexed_surface(const TSDFVolume& tsdf_volume, std::vector<float3>& verts, std::vector<float3>& normals,
+                              std::vector<int3>& triangles);
+
 }  // namespace cuphoto
 
 #endif

@@ -49,6 +49,9 @@ struct TSDFEngineOptions {
     r32 max_depth = 0.f;
     r32 min_z = 0.f;
     i32 memory = GBT_MEMORY_MANAGED;
+    // fixed mode: mesh with shared vertices and per-vertex normals
+    // (generate_indexed_surface) instead of three vertices per triangle
+    bool shared_vertices = false;
 };
 
 class cudaPointCloud;

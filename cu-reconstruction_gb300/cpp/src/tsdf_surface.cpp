@@ -63,6 +63,7 @@ TSDFSurface::TSDFSurface(const Config& cfg) {
                                                                                             : GBT_ARITH_REFERENCE;
     engine_options.truncation = cfg.get<r32>("tsdf.engine.truncation", 0.f);
     engine_options.max_depth = cfg.get<r32>("tsdf.engine.max_depth", 0.f);
+    engine_options.shared_vertices = cfg.get<std::string>("tsdf.engine.shared_vertices", "false") == "true";
 }
 
 void TSDFSurface::set_global_transformation(const SE3& transform) { global_transform = transform; }
@@ -80,7 +81,16 @@ std::array<r64, 7> TSDFSurface::global_pose() const {
 void TSDFSurface::mesh_from(const TSDFVolume& volume) {
     std::vector<float3> verts;
     std::vector<int3> triangles;
-    generate_triangular_surface(volume, verts, triangles);
+    if (engine_options.shared_vertices && engine_options.mode == GBT_MODE_FIXED) {
+        std::vector<float3> nrm;
+        if (generate_indexed_surface(volume, verts, nrm, triangles)) {
+            std::vector<Mesh::Normal> mesh_normals(nrm.size());
+            for (size_t i = 0; i < nrm.size(); ++i) mesh_normals[i] = Mesh::Normal(nrm[i].x, nrm[i].y, nrm[i].z, 0.f);
+            surface_mesh.normals(mesh_normals);
+        }
+    } else {
+        generate_triangular_surface(volume, verts, triangles);
+    }
     std::vector<Mesh::Point> mesh_verts(verts.size());
     std::vector<Mesh::Triangle> mesh_triangles(triangles.size());
     for (size_t i = 0; i < verts.size(); ++i) mesh_verts[i] = Mesh::Point(verts[i].x, verts[i].y, verts[i].z);

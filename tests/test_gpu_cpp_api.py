@@ -189,3 +189,45 @@ def test_headless_point_cloud_path(gpu, tmp_path):
     assert lines[9] == "end_header" and len(lines) == 10 + cam.width * cam.height
     assert counts["depth"] > 300, counts
     assert 0.5 * counts["depth"] <= counts["points"] <= 1.1 * counts["depth"], counts
+
+
+def read_binary_ply(path):
+    data = open(path, "rb").read()
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    header = data[:end].decode().splitlines()
+    nv = int([l for l in header if l.startswith("element vertex")][0].split()[-1])
+    nf = int([l for l in header if l.startswith("element face")][0].split()[-1])
+    vdt = np.dtype([("p", "<f4", 3), ("c", "u1", 3), ("n", "<f4", 4)])
+    V = np.frombuffer(data, vdt, nv, end)
+    F = np.frombuffer(data, np.dtype([("k", "u1"), ("i", "<i4", 3)]), nf, end + nv * vdt.itemsize)
+    assert np.all(F["k"] == 3)
+    return V, F["i"]
+
+
+@pytest.mark.gpu
+def test_headless_shared_vertex_mesh(gpu, tmp_path):
+    """tsdf.engine.shared_vertices: the fixed-mode mesh through
+    generate_indexed_surface, stored as a binary PLY with normals: the same
+    triangles as the three-vertices-per-triangle mesh, fewer vertices."""
+    cam = S.Camera.half()
+    seq = S.make_sequence(1, scene_id=3, camera=cam, trajectory="frontal")
+    grid, phys, off = (96, 80, 64), (1.6, 1.2, 1.28), (-0.8, -0.6, 0.3)
+    (tmp_path / "depth.u16").write_bytes(seq.depth_u16[0].astype("<u2").tobytes())
+    out = {}
+    for shared in ("false", "true"):
+        ply = str(tmp_path / ("m_%s.ply" % shared))
+        cfgp = str(tmp_path / ("c_%s.yaml" % shared))
+        write_config(cfgp, grid, phys, off, cam, ply, "tsdf.engine.mode: fixed\ntsdf.engine.shared_vertices: %s\n"
+                     % shared)
+        r = subprocess.run([EXAMPLE, "--config_path", cfgp, "--depth", str(tmp_path / "depth.u16")],
+                           capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+        out[shared] = ply
+    Vs, Fs = read_ply(out["false"])
+    V, F = read_binary_ply(out["true"])
+    assert len(F) == len(Fs) > 300
+    assert len(V) < 0.6 * len(Vs)
+    # the same triangles: gather the shared vertices back (PLY text has 6 digits)
+    np.testing.assert_allclose(V["p"][F].reshape(-1, 3), Vs[Fs.reshape(-1)], rtol=0, atol=1e-5)
+    n = np.linalg.norm(V["n"][:, :3], axis=1)
+    assert np.all(np.abs(n - 1) < 1e-5)
