@@ -354,7 +354,8 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     const int64_t ncubes = (d.nx >= 2 && d.ny >= 2 && d.nz >= 2)
                                ? (int64_t)(d.nx - 1) * (d.ny - 1) * (d.nz - 1) : 0;
     a->ncubes = (uint32_t)ncubes;
-    a->ntiles = (uint32_t)((ncubes + gbt::kMcTile - 1) / gbt::kMcTile);
+    const int64_t tile = gbt::mc_tile_cubes(v->cfg.mode);
+    a->ntiles = (uint32_t)((ncubes + tile - 1) / tile);
     a->div_cx = gbt::make_fastdiv((uint32_t)(d.nx > 1 ? d.nx - 1 : 1));
     a->div_cy = gbt::make_fastdiv((uint32_t)(d.ny > 1 ? d.ny - 1 : 1));
     a->div_gx = gbt::make_fastdiv((uint32_t)d.nx);

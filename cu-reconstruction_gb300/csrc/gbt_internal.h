@@ -90,10 +90,13 @@ inline FastDiv make_fastdiv(uint32_t d) {
 }
 
 // Marching cubes over the linear cube order (z, y, x), one tile of
-// kMcTile cubes per CTA, tiles chained by a decoupled look-back.
+// mc_tile_cubes(mode) cubes per CTA and tile, tiles chained by a decoupled look-back.
 constexpr int kMcThreads = 256;
-constexpr int kMcCubesPerThread = 4;
-constexpr int kMcTile = kMcThreads * kMcCubesPerThread;
+// Cubes per thread per tile: 8 in the compat mode (one D load per corner), 4
+// in the fixed mode (which also loads W, and keeps twice the values in flight).
+__host__ __device__ constexpr int mc_cubes_per_thread(int mode) { return mode == 1 ? 4 : 8; }
+__host__ __device__ constexpr int mc_tile_cubes(int mode) { return kMcThreads * mc_cubes_per_thread(mode); }
+constexpr int kMcTileMin = kMcThreads * 4;   // the smallest tile of either mode
 
 struct McArgs {
     const float* D;

@@ -568,12 +568,62 @@ __device__ __forceinline__ int64_t weld_edge_id(const McArgs& a, uint32_t cx, ui
     return 3 * lin + axis;
 }
 
+// Cube types (the 8-bit corner sign pattern, 0 for a cube that is not
+// emitted) of cubes i0 .. i0+3 of the thread's cubes in a tile.  Every corner
+// load of the batch is issued before any is used; a cube past the end reads
+// the last cube, in bounds, and is discarded.
+template <int MODE, int CPT>
+__device__ __forceinline__ void mc_classify4(const McArgs& a, uint32_t tile, int tid, int i0, int (&type)[CPT]) {
+    const uint32_t c0 = tile * (uint32_t)(kMcThreads * CPT);
+    float dv[4][8];
+    float wv[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        uint32_t c = c0 + (i0 + i) * kMcThreads + tid;
+        c = c < a.ncubes ? c : a.ncubes - 1;
+        const uint32_t row = fastdiv(c, a.div_cx);
+        const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
+        const uint32_t cz = fastdiv(row, a.div_cy);
+        const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+        int64_t b0, b1;
+        cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int64_t idx = corner_index<MODE>(a, b0, b1, k);
+            dv[i][k] = __ldg(a.D + idx);
+            if (MODE == kFixed) wv[i][k] = __ldg(a.W + idx);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        int t = 0;
+        bool ok = c0 + (i0 + i) * kMcThreads + tid < a.ncubes;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (dv[i][k] < 0.f) t |= 1 << k;
+            if (MODE == kFixed) ok &= wv[i][k] > 0.f;
+        }
+        type[i0 + i] = ok ? t : 0;
+    }
+}
+
+// Single-pass marching cubes over tiles of mc_tile_cubes(MODE) cubes taken by ticket.
+// Per tile: classify (corner loads batched four cubes at a time), warp scans
+// of the triangle counts, warp 0 scans the partial sums and looks back over
+// the preceding tiles for the tile's offset, then every thread emits its
+// cubes' triangles straight to their final positions.
 template <int MODE>
 __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McArgs a) {
     __shared__ unsigned char s_count[256];
     __shared__ unsigned long long s_tri[256];
     __shared__ unsigned char s_ends[12];
-    __shared__ int s_wsum[kMcCubesPerThread * (kMcThreads / 32)];
+    constexpr int kWarps = kMcThreads / 32;
+    constexpr int CPT = mc_cubes_per_thread(MODE);
+    constexpr int kTile = kMcThreads * CPT;
+    constexpr int kParts = CPT * kWarps;   // partial sums per tile, in linear cube order
+    static_assert(kParts % 32 == 0 && kParts <= 32 * 4, "warp 0 scans the partial sums, up to 4 per lane");
+    constexpr int kPerLane = kParts / 32;
+    __shared__ int s_wsum[kParts];
     __shared__ unsigned int s_tile;
     __shared__ long long s_prefix;
 
@@ -584,7 +634,6 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
     }
     if (tid < 12) s_ends[tid] = GBT_MC_EDGE_ENDS[tid];
     const int lane = tid & 31, warp = tid >> 5;
-    constexpr int kWarps = kMcThreads / 32;
 
     for (;;) {
         __syncthreads();
@@ -592,32 +641,15 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= a.ntiles) return;
-        const uint32_t c0 = tile * (uint32_t)kMcTile;
+        const uint32_t c0 = tile * (uint32_t)kTile;
 
-        int type[kMcCubesPerThread];
-        int incl[kMcCubesPerThread];
+        int type[CPT];
+        int incl[CPT];
 #pragma unroll
-        for (int i = 0; i < kMcCubesPerThread; ++i) {
-            const uint32_t c = c0 + i * kMcThreads + tid;
-            int t = 0;
-            if (c < a.ncubes) {
-                const uint32_t row = fastdiv(c, a.div_cx);
-                const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
-                const uint32_t cz = fastdiv(row, a.div_cy);
-                const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
-                int64_t b0, b1;
-                cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
-                bool ok = true;
+        for (int i0 = 0; i0 < CPT; i0 += 4) mc_classify4<MODE, CPT>(a, tile, tid, i0, type);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int64_t idx = corner_index<MODE>(a, b0, b1, k);
-                    if (MODE == kFixed) ok = ok && (__ldg(a.W + idx) > 0.f);
-                    if (__ldg(a.D + idx) < 0.f) t |= 1 << k;
-                }
-                if (!ok) t = 0;
-            }
-            type[i] = t;
-            int n = s_count[t];
+        for (int i = 0; i < CPT; ++i) {
+            int n = s_count[type[i]];
             // inclusive warp scan
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -629,18 +661,27 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
         }
         __syncthreads();
         if (warp == 0) {
-            // exclusive scan of the (i, warp) partial sums, in linear cube order
-            constexpr int kParts = kMcCubesPerThread * kWarps;
-            static_assert(kParts <= 32, "one warp scans the partial sums");
-            int s = lane < kParts ? s_wsum[lane] : 0;
-            int x = s;
+            // exclusive scan of the kParts partial sums, kPerLane consecutive ones per lane
+            int v[kPerLane];
+            int local = 0;
+#pragma unroll
+            for (int q = 0; q < kPerLane; ++q) {
+                v[q] = s_wsum[lane * kPerLane + q];
+                local += v[q];
+            }
+            int x = local;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
             const int total = __shfl_sync(0xffffffffu, x, 31);
-            if (lane < kParts) s_wsum[lane] = x - s;
+            int run = x - local;
+#pragma unroll
+            for (int q = 0; q < kPerLane; ++q) {
+                s_wsum[lane * kPerLane + q] = run;
+                run += v[q];
+            }
             // decoupled look-back over the preceding tiles, 32 at a time: lane
             // l reads tile (j - l); the nearest tile with an inclusive prefix
             // ends the walk, the aggregates before it are summed by the warp
@@ -667,10 +708,10 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
                     if (failed) break;
                     const unsigned incl_lanes = __ballot_sync(0xffffffffu, (w & ~kValueMask) == kFlagIncl);
                     const int stop = incl_lanes ? __ffs(incl_lanes) - 1 : 31;   // nearest inclusive tile
-                    long long v = lane <= stop ? (long long)(w & kValueMask) : 0;
+                    long long sv = lane <= stop ? (long long)(w & kValueMask) : 0;
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    prefix += v;
+                    for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+                    prefix += sv;
                     if (incl_lanes) break;
                     j -= 32;
                 }
@@ -686,11 +727,10 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
             }
         }
         __syncthreads();
-        if (a.cap <= 0) continue;
         const long long tile_prefix = s_prefix;
 
 #pragma unroll
-        for (int i = 0; i < kMcCubesPerThread; ++i) {
+        for (int i = 0; i < CPT; ++i) {
             const int t = type[i];
             const int n = s_count[t];
             if (!n) continue;
@@ -800,7 +840,7 @@ __global__ void __launch_bounds__(256) weld_mark_kernel(const __grid_constant__ 
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int64_t idx = corner_index<kFixed>(a, b0, b1, k);
-            ok = ok && (__ldg(a.W + idx) > 0.f);
+            ok &= __ldg(a.W + idx) > 0.f;
             if (__ldg(a.D + idx) < 0.f) t |= 1 << k;
         }
         if (!ok) continue;

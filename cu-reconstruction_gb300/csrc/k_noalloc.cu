@@ -20,7 +20,7 @@
 namespace {
 
 // [0, 64): tile ticket (u32), look-back error flag (i32), triangle total (i64);
-// then one look-back status word (u64) per tile of kMcTile cubes.
+// then one look-back status word (u64) per tile (at least 1024 cubes).
 static __device__ __align__(256) unsigned char g_mesh_scratch[GBT_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
@@ -93,7 +93,8 @@ gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, 
         a.off[i] = d.off[i];
     }
     a.ncubes = (uint32_t)ncubes;
-    a.ntiles = (uint32_t)((ncubes + gbt::kMcTile - 1) / gbt::kMcTile);
+    const int64_t tile = gbt::mc_tile_cubes(gbt::volume_mode(v));
+    a.ntiles = (uint32_t)((ncubes + tile - 1) / tile);
     a.div_cx = gbt::make_fastdiv((uint32_t)(d.nx > 1 ? d.nx - 1 : 1));
     a.div_cy = gbt::make_fastdiv((uint32_t)(d.ny > 1 ? d.ny - 1 : 1));
     a.div_gx = gbt::make_fastdiv((uint32_t)d.nx);
