@@ -129,6 +129,8 @@ gbt_status check_frames(const gbt_frame* frames, int32_t nframes) {
             return fail(GBT_ERR_INVALID_ARG, "frame %d: pitch %zu below width*%zu", i, f.pitch_bytes, elem);
         if (f.pitch_bytes % elem != 0 || ((uintptr_t)f.depth % elem) != 0)
             return fail(GBT_ERR_INVALID_ARG, "frame %d: depth rows not aligned to the element size", i);
+        if ((uint64_t)f.height * (f.pitch_bytes / elem) > 0xffffffffull)
+            return fail(GBT_ERR_INVALID_ARG, "frame %d: image larger than 2^32 elements", i);
         for (int k = 0; k < 7; ++k)
             if (!std::isfinite(f.pose[k])) return fail(GBT_ERR_INVALID_ARG, "frame %d: pose is not finite", i);
     }

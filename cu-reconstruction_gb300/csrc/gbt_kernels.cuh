@@ -273,8 +273,13 @@ template <int MODE>
 __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& fd, const float* pr, const float* px,
                                             float py, float pz, int nvalid, float* d, float* w, const float* s_inv) {
     bool dirty = false;
-    const char* dimg = static_cast<const char*>(fd.depth);
-    const int64_t pitch = fd.pitch;
+    // pixel (u, v) is element v * pitch_elems + u of the image (the host checks
+    // that height * pitch_elems fits 32 bits and that the pitch is a whole
+    // number of elements)
+    const bool u16 = fd.fmt == GBT_DEPTH_U16;
+    const unsigned short* d16 = static_cast<const unsigned short*>(fd.depth);
+    const float* d32 = static_cast<const float*>(fd.depth);
+    const uint32_t pitch_elems = (uint32_t)(u16 ? (fd.pitch >> 1) : (fd.pitch >> 2));
     const uint32_t width = (uint32_t)fd.width, height = (uint32_t)fd.height;
     if (MODE == kCompat) {
         const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
@@ -303,15 +308,14 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
         for (int i = 0; i < 4; ++i) {
             if (i >= nvalid) break;
             const int u = pu[i], vv = pv[i];
-            // tsdf_volume.cu:166-187
-            if (u < 0 || (uint32_t)u >= width || vv < 0 || (uint32_t)vv >= height) continue;
-            const char* row = dimg + (int64_t)vv * pitch;
+            // tsdf_volume.cu:166-187 (negative u, v wrap to large unsigned values)
+            if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
+            const uint32_t pix = (uint32_t)vv * pitch_elems + (uint32_t)u;
             // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
             // (rgbd_dataset.cpp:29): one float multiply
-            const float dv = fd.fmt == GBT_DEPTH_U16
-                                 ? u16_metres(__ldg(reinterpret_cast<const unsigned short*>(row) + u), fd.scale)
-                                 : __ldg(reinterpret_cast<const float*>(row) + u);
-            if (dv <= 0.0f || dv > 24.0) continue;
+            const float dv = u16 ? u16_metres(__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
+            // 24 is exact in float, so this is the reference's double comparison
+            if (dv <= 0.0f || dv > 24.0f) continue;
             const float sdf = dv - pz;
             if (sdf >= -v.trunc) {
                 float tsdf = sdf;
@@ -328,7 +332,6 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
         const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
         const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
         const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
-        const int fmt = fd.fmt;
         const float scale = fd.scale;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -341,12 +344,8 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
             const int u = __float2int_rn(__fmul_rn(U, rz));
             const int vv = __float2int_rn(__fmul_rn(V, rz));
             if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
-            const char* row = dimg + (int64_t)vv * pitch;
-            float dv;
-            if (fmt == GBT_DEPTH_U16)
-                dv = __fmul_rn((float)__ldg(reinterpret_cast<const unsigned short*>(row) + u), scale);
-            else
-                dv = __ldg(reinterpret_cast<const float*>(row) + u);
+            const uint32_t pix = (uint32_t)vv * pitch_elems + (uint32_t)u;
+            const float dv = u16 ? __fmul_rn((float)__ldg(d16 + pix), scale) : __ldg(d32 + pix);
             if (!(dv > 0.f && dv <= v.max_depth)) continue;
             const float sdf = __fsub_rn(dv, Z);
             if (!(sdf >= -v.trunc)) continue;
