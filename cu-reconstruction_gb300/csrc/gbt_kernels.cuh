@@ -268,11 +268,15 @@ __device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const Fra
     return __ballot_sync(0xffffffffu, live);
 }
 
-// Applies one frame to the thread's (up to) 4 voxels; returns whether any changed.
+// One frame's samples for the thread's (up to) 4 voxels: the depth under
+// each voxel, 0 where the voxel projects off the image (or, in the fixed
+// mode, lies at or in front of min_z) -- values the update skips -- and, in
+// the fixed mode, the voxel's camera z.  Split from the update so that the
+// next frame's depth gathers are in flight while this frame's running
+// averages are computed.
 template <int MODE>
-__device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& fd, const float* pr, const float* px,
-                                            float py, float pz, int nvalid, float* d, float* w, const float* s_inv) {
-    bool dirty = false;
+__device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc& fd, const float* pr, const float* px,
+                                              float py, float pz, int nvalid, float (&dv)[4], float (&zc)[4]) {
     // pixel (u, v) is element v * pitch_elems + u of the image (the host checks
     // that height * pitch_elems fits 32 bits and that the pitch is a whole
     // number of elements)
@@ -306,17 +310,53 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            if (i >= nvalid) break;
-            const int u = pu[i], vv = pv[i];
-            // tsdf_volume.cu:166-187 (negative u, v wrap to large unsigned values)
+            dv[i] = 0.f;
+            // tsdf_volume.cu:166-170 (negative u, v wrap to large unsigned values)
+            if (i < nvalid && (uint32_t)pu[i] < width && (uint32_t)pv[i] < height) {
+                const uint32_t pix = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
+                // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
+                // (rgbd_dataset.cpp:29): one float multiply
+                dv[i] = u16 ? u16_metres(__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
+            }
+        }
+    } else {
+#if !defined(GBT_REF_ARITH)
+        const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
+        const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
+        const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            dv[i] = 0.f;
+            const float Z = __fmaf_rn(pr[8], px[i], aZ);
+            zc[i] = Z;
+            if (i >= nvalid || !(Z > v.min_z)) continue;
+            const float U = __fmaf_rn(pr[0], px[i], aU);
+            const float V = __fmaf_rn(pr[4], px[i], aV);
+            const float rz = __frcp_rn(Z);
+            const int u = __float2int_rn(__fmul_rn(U, rz));
+            const int vv = __float2int_rn(__fmul_rn(V, rz));
             if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
             const uint32_t pix = (uint32_t)vv * pitch_elems + (uint32_t)u;
-            // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
-            // (rgbd_dataset.cpp:29): one float multiply
-            const float dv = u16 ? u16_metres(__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
-            // 24 is exact in float, so this is the reference's double comparison
-            if (dv <= 0.0f || dv > 24.0f) continue;
-            const float sdf = dv - pz;
+            dv[i] = u16 ? __fmul_rn((float)__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
+        }
+#endif
+    }
+}
+
+// One frame's running-average update of the thread's voxels from its
+// samples; returns whether any voxel changed.
+template <int MODE>
+__device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)[4], const float (&zc)[4], float pz,
+                                             int nvalid, float* d, float* w, const float* s_inv) {
+    bool dirty = false;
+    if (MODE == kCompat) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i >= nvalid) break;
+            // tsdf_volume.cu:171-187; 24 is exact in float, so this is the
+            // reference's double comparison
+            if (dv[i] <= 0.0f || dv[i] > 24.0f) continue;
+            const float sdf = dv[i] - pz;
             if (sdf >= -v.trunc) {
                 float tsdf = sdf;
                 if (sdf > 0) tsdf = fminf(sdf, v.trunc);
@@ -329,25 +369,11 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
         }
     } else {
 #if !defined(GBT_REF_ARITH)
-        const float aU = __fmaf_rn(pr[1], py, __fmaf_rn(pr[2], pz, pr[3]));
-        const float aV = __fmaf_rn(pr[5], py, __fmaf_rn(pr[6], pz, pr[7]));
-        const float aZ = __fmaf_rn(pr[9], py, __fmaf_rn(pr[10], pz, pr[11]));
-        const float scale = fd.scale;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (i >= nvalid) break;
-            const float Z = __fmaf_rn(pr[8], px[i], aZ);
-            if (!(Z > v.min_z)) continue;
-            const float U = __fmaf_rn(pr[0], px[i], aU);
-            const float V = __fmaf_rn(pr[4], px[i], aV);
-            const float rz = __frcp_rn(Z);
-            const int u = __float2int_rn(__fmul_rn(U, rz));
-            const int vv = __float2int_rn(__fmul_rn(V, rz));
-            if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
-            const uint32_t pix = (uint32_t)vv * pitch_elems + (uint32_t)u;
-            const float dv = u16 ? __fmul_rn((float)__ldg(d16 + pix), scale) : __ldg(d32 + pix);
-            if (!(dv > 0.f && dv <= v.max_depth)) continue;
-            const float sdf = __fsub_rn(dv, Z);
+            if (!(dv[i] > 0.f && dv[i] <= v.max_depth)) continue;
+            const float sdf = __fsub_rn(dv[i], zc[i]);
             if (!(sdf >= -v.trunc)) continue;
             const float tsdf = fminf(sdf, v.trunc);
             const int n = max(__float2int_rz(w[i]), 0) + 1;
@@ -357,6 +383,38 @@ __device__ __forceinline__ bool apply_frame(const VolDesc& v, const FrameDesc& f
             dirty = true;
         }
 #endif
+    }
+    return dirty;
+}
+
+// Applies the frames of `mask` (bit f: frames[f], poses[f]) in order to the
+// thread's voxels, the next frame's samples gathered before the current
+// frame's update; returns whether any voxel changed.
+template <int MODE>
+__device__ __forceinline__ bool apply_frames(const VolDesc& v, const FrameDesc* frames, const float (*poses)[12],
+                                             uint32_t mask, int fbase, const float* px, float py, float pz,
+                                             int nvalid, float* d, float* w, const float* s_inv) {
+    if (!mask) return false;
+    bool dirty = false;
+    float dv[4], zc[4];
+    int f = __ffs(mask) - 1;
+    mask &= mask - 1;
+    frame_samples<MODE>(v, frames[fbase + f], poses[fbase + f], px, py, pz, nvalid, dv, zc);
+    for (;;) {
+        float dvn[4], zcn[4];
+        const bool more = mask != 0u;
+        if (more) {
+            f = __ffs(mask) - 1;
+            mask &= mask - 1;
+            frame_samples<MODE>(v, frames[fbase + f], poses[fbase + f], px, py, pz, nvalid, dvn, zcn);
+        }
+        dirty |= frame_update<MODE>(v, dv, zc, pz, nvalid, d, w, s_inv);
+        if (!more) break;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            dv[i] = dvn[i];
+            zc[i] = zcn[i];
+        }
     }
     return dirty;
 }
@@ -444,10 +502,14 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
         ThreadVoxels t;
         if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
         t.load(v);
+        // frame by frame (the pipelined apply_frames costs this kernel more in
+        // occupancy than it gains; the batched kernel uses it)
         bool dirty = false;
         for (uint32_t m = fmask; m; m &= m - 1) {
             const int f = __ffs(m) - 1;
-            dirty |= apply_frame<MODE>(v, a.frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, t.d, t.w, s_inv);
+            float dv[4], zc[4];
+            frame_samples<MODE>(v, a.frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, dv, zc);
+            dirty |= frame_update<MODE>(v, dv, zc, t.pz, t.nvalid, t.d, t.w, s_inv);
         }
         if (dirty) t.store(v);
     }
@@ -514,10 +576,8 @@ __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_const
         bool dirty = false;
 #pragma unroll
         for (int c = 0; c < kBatchMaxFrames / 32; ++c)
-            for (uint32_t m = masks[c]; m; m &= m - 1) {
-                const int f = c * 32 + __ffs(m) - 1;
-                dirty |= apply_frame<MODE>(v, frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, t.d, t.w, s_inv);
-            }
+            dirty |= apply_frames<MODE>(v, frames, s_pose, masks[c], c * 32, t.px, t.py, t.pz, t.nvalid, t.d, t.w,
+                                        s_inv);
         if (dirty) t.store(v);
     }
 }
