@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--mode", default="compat", choices=["compat", "fixed"])
     ap.add_argument("--grid", type=int, default=None, help="default 512 (batched), 1024 (refine)")
     ap.add_argument("--frames", type=int, default=None, help="default 300 (batched), 1000 (refine)")
+    ap.add_argument("--split-scenes", action="store_true",
+                    help="multiscene under torchrun: split one set of 16 scenes over the ranks (strong scaling)")
     ap.add_argument("--refine-steps", type=int, default=50)
     ap.add_argument("--refine-frames", type=int, default=64)
     ap.add_argument("--refine-trunc", type=float, default=0.04, help="truncation (m) of the refinement volumes")
@@ -696,19 +698,27 @@ def multiscene(args, torch, rank, world, local):
     """16 independent seeded scenes, grids drawn from 64^3..384^3 (multiples of
     8), 10..120 frames of 640x480 each, all integrated by the batched launches
     in one captured graph, then a mesh per scene.  With N ranks every rank
-    runs its own 16 scenes (seeds offset by rank)."""
+    runs its own 16 scenes (seeds offset by rank; weak scaling), or, with
+    --split-scenes, the ranks split one set of 16 scenes balanced by
+    voxel-updates (strong scaling)."""
     import ctypes as C
     from cuphoto import TSDFVolume, TSDFVolumeConfig, extract_mesh_device
     from cuphoto import _lib as L
     from cuphoto import synthetic as S
     from cuphoto.batch import BatchIntegrator
-    rng = np.random.default_rng(77 + rank)
+    from cuphoto import shard
+    split = args.split_scenes and world > 1
+    rng = np.random.default_rng(77 if split else 77 + rank)
+    specs = [(int(rng.integers(8, 49)) * 8, int(rng.integers(10, 121))) for _ in range(16)]
+    if split:
+        mine = shard.partition_by_cost([n ** 3 * f for n, f in specs], world)[rank]
+    else:
+        mine = list(range(16))
     cam = S.Camera()
     vols, depths, poses, sizes, nfs = [], [], [], [], []
-    for i in range(16):
-        n = int(rng.integers(8, 49)) * 8
-        nf = int(rng.integers(10, 121))
-        sid = 100 * rank + i
+    for i in mine:
+        n, nf = specs[i]
+        sid = i if split else shard.scene_seed(0, rank, i)
         scene = S.make_scene(scene_id=sid)
         ps = S.circle_poses(nf, phase=0.1 * i)
         fr = S.render_sequence_torch(scene, ps, cam, seed=sid)
@@ -720,7 +730,7 @@ def multiscene(args, torch, rank, world, local):
         sizes.append(n)
         nfs.append(nf)
     updates = sum(n ** 3 * f for n, f in zip(sizes, nfs))
-    batch = BatchIntegrator(max_scenes=16, max_frames=sum(nfs))
+    batch = BatchIntegrator(max_scenes=len(vols), max_frames=sum(nfs))
     # autotune: brick x frames per launch x CTAs/SM on the whole batch
     if args.config:
         brick, fpl, ctas = (int(x) for x in args.config.split(","))
@@ -780,8 +790,7 @@ def multiscene(args, torch, rank, world, local):
         g_mesh.replay()
     torch.cuda.synchronize()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
+    shard.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         for i in range(args.steps):
@@ -791,11 +800,8 @@ def multiscene(args, torch, rank, world, local):
             g_mesh.replay()
             ev[i][2].record(stream)
         torch.cuda.synchronize()
-    total_ms = ev[0][0].elapsed_time(ev[-1][2])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = shard.max_over_ranks(ev[0][0].elapsed_time(ev[-1][2]))
+    job_updates = shard.sum_over_ranks(updates)
     int_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
     mesh_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
     ntri = sum(int(o[2].item()) for o in outs)
@@ -827,24 +833,27 @@ def multiscene(args, torch, rank, world, local):
         if i >= args.warmup:
             e2e.append(time.perf_counter() - t0)
     h2d = sum(d.numel() * d.element_size() for ds in depths for d in ds)
-    value = world * updates * args.steps / (total_ms * 1e-3)
+    value = job_updates * args.steps / (total_ms * 1e-3)
+    e2e_value = shard.whole_job_rate(updates, float(np.mean(e2e)))
     if rank != 0:
         return None
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "strong" if split else "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: 16 seeded plane + 6 sphere scenes, ray-cast uint16 depth, circle poses",
-        "config": {"workload": "multi-scene batched integrate + marching cubes: 16 volumes %s^3, %s frames 640x480"
-                               % (sizes, nfs),
+        "config": {"workload": "multi-scene batched integrate + marching cubes: %d volumes %s^3, %s frames 640x480"
+                               "%s" % (len(vols), sizes, nfs, " (rank 0's share of 16 split over %d ranks)" % world
+                                       if split else ""),
                    "mode": args.mode, "frames_per_launch": fpl, "brick": brick, "ctas_per_sm": ctas,
                    "voxel_updates_per_step": updates, "graph": "resets + batched launches, meshes: CUDA graphs",
                    "triangles": ntri},
         "breakdown_ms": {"integrate": int_ms, "mesh": mesh_ms},
         "integrate_only": {"value": updates / (int_ms * 1e-3), "unit": UNIT},
         "per_scene": per_scene,
-        "e2e": {"value": world * updates / float(np.mean(e2e)), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e))},
-        "gpu_launches": args.steps * (16 + ((max(nfs) + fpl - 1) // fpl) + 16),
+        "gpu_launches": args.steps * (2 * len(vols) + ((max(nfs) + fpl - 1) // fpl)),
         "clocks": clocks.summary(),
         "autotune": {"candidates": len(table)},
     }
@@ -1004,11 +1013,8 @@ def main():
     step_ms = [ev[i][0].elapsed_time(ev[i][3]) for i in range(args.steps)]
     int_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
     mesh_ms = [ev[i][2].elapsed_time(ev[i][3]) for i in range(args.steps)]
-    total_ms = ev[0][0].elapsed_time(ev[-1][3])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from cuphoto import shard
+    total_ms = shard.max_over_ranks(ev[0][0].elapsed_time(ev[-1][3]))
     ntri = int(count.item())
     value = world * nvox * nf * args.steps / (total_ms * 1e-3)
 
@@ -1037,7 +1043,7 @@ def main():
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
             d2h = Vh.numel() * 4 + Th.numel() * 4 + 8
-    e2e_value = world * nvox * nf / (float(np.mean(e2e_ms)) * 1e-3)
+    e2e_value = shard.whole_job_rate(nvox * nf, float(np.mean(e2e_ms)) * 1e-3)
 
     if rank != 0:
         if world > 1:
