@@ -212,7 +212,7 @@ def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=3):
 
     def integ():
         vf.reset()
-        vf.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+        vf.integrate_sequence(depths, poses, frames_per_pass=min(K, 32), brick=brick, ctas_per_sm=ctas)
 
     def timed(fn):
         fn()
@@ -930,7 +930,8 @@ def main():
     import ctypes as C
     from cuphoto import TSDFVolume, extract_mesh_device, make_frame
     from cuphoto import _lib as L
-    from cuphoto.autotune import tune_integrate
+    from cuphoto.autotune import tune_batched, tune_integrate
+    from cuphoto.batch import BatchIntegrator
 
     S, cam, scene, poses = workload(args, rank)
     nf = len(poses)
@@ -943,17 +944,51 @@ def main():
     vol = TSDFVolume(tc)
     depths = [frames_dev[k] for k in range(nf)]
 
+    # two paths of the engine integrate one volume: passes of up to 32 frames
+    # (gbt_integrate) and the batched launch with windows of up to 128 frames
+    # (gbt_integrate_batch with this one volume); each is autotuned and the
+    # faster on the whole sequence is timed
+    batch = BatchIntegrator(max_scenes=1, max_frames=nf)
     if args.config:
-        b_, k_, c_ = (int(x) for x in args.config.split(","))
+        parts = args.config.split(",")
+        b_, k_, c_ = (int(x) for x in parts[:3])
+        path = parts[3] if len(parts) > 3 else "single"
         tune = {"brick": b_, "frames": k_, "ctas": c_, "ns_per_update": None, "table": []}
+        candidates = 0
     else:
-        tune = tune_integrate(vol, depths, poses)
+        t_single = tune_integrate(vol, depths, poses)
+        t_batched = tune_batched(vol, depths, poses, batch)
+        candidates = len(t_single["table"]) + len(t_batched["table"])
+
+        def full_ms(fn):
+            fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(2):
+                fn()
+            e1.record()
+            e1.synchronize()
+            return e0.elapsed_time(e1) / 2
+
+        ms_single = full_ms(lambda: (vol.reset(), vol.integrate_sequence(
+            depths, poses, frames_per_pass=t_single["frames"], brick=t_single["brick"],
+            ctas_per_sm=t_single["ctas"])))
+        ms_batched = full_ms(lambda: (vol.reset(), batch.integrate(
+            [vol], [depths], [poses], brick=t_batched["brick"], ctas_per_sm=t_batched["ctas"],
+            frames_per_launch=t_batched["frames"])))
+        path, tune = ("batched", t_batched) if ms_batched < ms_single else ("single", t_single)
     K, brick, ctas = tune["frames"], tune["brick"], tune["ctas"]
     n_passes = (nf + K - 1) // K
 
+    def integrate_all():
+        if path == "batched":
+            batch.integrate([vol], [depths], [poses], brick=brick, ctas_per_sm=ctas, frames_per_launch=K)
+        else:
+            vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+
     # mesh capacity from an untimed run
     vol.reset()
-    vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+    integrate_all()
     V0, T0 = extract_mesh_device(vol)
     cap = max(1024, int(len(V0) * 1.25) + 1024)
     verts = torch.empty((cap, 3, 3), dtype=torch.float32, device="cuda")
@@ -965,7 +1000,7 @@ def main():
         vol.reset()
 
     def step_integrate():
-        vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+        integrate_all()
 
     def step_mesh():
         L.check(lib.gbt_extract_mesh_async(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
@@ -1035,7 +1070,7 @@ def main():
         t0 = time.perf_counter()
         frames_dev.copy_(frames_host, non_blocking=True)
         vol.reset()
-        vol.integrate_sequence(depths, poses, frames_per_pass=K, brick=brick, ctas_per_sm=ctas)
+        integrate_all()
         V, T = extract_mesh_device(vol, capacity=cap)
         Vh = V.cpu()
         Th = T.cpu()
@@ -1063,12 +1098,14 @@ def main():
         "dtype": "f32", "data": "synthetic: seeded plane + 6 spheres, ray-cast uint16 depth, helix trajectory",
         "config": {"workload": "batched integrate + marching cubes, %d^3 voxels of %.2g cm, %d frames 640x480 uint16"
                                % (args.grid, 256.0 / args.grid, nf),
-                   "mode": args.mode, "frames_per_pass": K, "brick": brick, "ctas_per_sm": ctas,
+                   "mode": args.mode, "path": path, "frames_per_pass": K, "brick": brick, "ctas_per_sm": ctas,
                    "passes_per_step": n_passes, "graph": "reset, integrate passes, mesh captured as CUDA graphs",
                    "l2": "inputs larger than L2: 1 GiB volume + %d MB depth per step" % (frames_dev.numel() * 2 // 2**20),
                    "triangles": ntri},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "integrate_kernel", "launch_ms": launch_ms,
+                     "traffic": None,
+                     "kernel": "integrate_batch_kernel" if path == "batched" else "integrate_kernel",
+                     "launch_ms": launch_ms,
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind},
         "breakdown_ms": {"reset": float(np.mean([ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)])),
                          "integrate": float(np.mean(int_ms)), "mesh": float(np.mean(mesh_ms))},
@@ -1079,7 +1116,7 @@ def main():
         "gpu_launches": args.steps * (1 + n_passes + 1),
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
-        "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": len(tune["table"])},
+        "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": candidates},
     }
     if cpu is not None:
         out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -83,3 +83,52 @@ def tune_integrate(vol, depths, poses, depth_scale=0.001, bricks=BRICKS, frames=
         cache[key] = res
         _store(cache)
     return res
+
+
+WINDOWS = (32, 64, 128)
+
+
+def tune_batched(vol, depths, poses, batch, depth_scale=0.001, bricks=(0, 1, 2, 3), windows=WINDOWS, ctas=(8, 16),
+                 repeats=2, use_cache=True):
+    """The same search for the batched path (gbt_integrate_batch with this one
+    volume): brick shape x frames per launch window x CTAs per SM, timed on
+    the whole sequence.  Returns {"brick", "frames", "ctas", "ns_per_update",
+    "table"}; "frames" is the window."""
+    import torch
+    h, w = int(depths[0].shape[0]), int(depths[0].shape[1])
+    key = _key(vol, w, h) + "|batched|%d" % len(depths)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        return cache[key]
+    nvox = 1
+    for g in vol.voxel_grid_size():
+        nvox *= g
+    table = []
+    best = None
+    stream = torch.cuda.current_stream()
+    for k in windows:
+        for b in bricks:
+            for c in ctas:
+                def run():
+                    vol.reset()
+                    batch.integrate([vol], [depths], [poses], depth_scale=depth_scale, brick=b, ctas_per_sm=c,
+                                    frames_per_launch=k)
+                run()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(repeats):
+                    run()
+                e1.record(stream)
+                e1.synchronize()
+                ns = e0.elapsed_time(e1) * 1e6 / (repeats * len(depths) * nvox)
+                table.append((b, k, c, ns))
+                if best is None or ns < best[3]:
+                    best = (b, k, c, ns)
+    vol.reset()
+    torch.cuda.synchronize()
+    res = {"brick": best[0], "frames": best[1], "ctas": best[2], "ns_per_update": best[3], "table": table}
+    if use_cache:
+        cache[key] = res
+        _store(cache)
+    return res
