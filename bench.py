@@ -1058,6 +1058,11 @@ def main():
     frame_px = cam.width * cam.height
     alg_bytes = 16.0 * nvox + (nf / n_passes) * frame_px * 2 + (nf / n_passes) * 64
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    # DRAM bytes per launch: one ncu capture of integrate_batch_kernel at 320^3
+    # with a 64-frame window read and wrote 274.0 + 168.4 MB (bricks no frame
+    # sees are not loaded, unchanged ones not stored), i.e. 13.50 B per voxel;
+    # scaled by voxels for the same window.  Other configurations: not measured.
+    traffic = 442.45e6 / 320 ** 3 * nvox if (path == "batched" and K == 64 and args.mode == "compat") else None
     peak, peak_kind = peaks()
 
     # end to end through the public API with host buffers: H2D of the step's
@@ -1103,7 +1108,7 @@ def main():
                    "l2": "inputs larger than L2: 1 GiB volume + %d MB depth per step" % (frames_dev.numel() * 2 // 2**20),
                    "triangles": ntri},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None,
+                     "traffic": traffic,
                      "kernel": "integrate_batch_kernel" if path == "batched" else "integrate_kernel",
                      "launch_ms": launch_ms,
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind},
