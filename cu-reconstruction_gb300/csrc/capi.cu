@@ -168,6 +168,16 @@ gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume
         return fail(GBT_ERR_INVALID_ARG, "fixed mode needs max_weight >= 1");
     if (!std::isfinite(c.focal_x) || !std::isfinite(c.focal_y) || !std::isfinite(c.cx) || !std::isfinite(c.cy))
         return fail(GBT_ERR_INVALID_ARG, "intrinsics not finite");
+    if (!(c.truncation > 0.f)) {
+        // the integrate kernels rely on a positive truncation distance
+        float dot = 0.f;
+        for (int i = 0; i < 3; ++i) {
+            const float vs = c.physical_size[i] / (float)c.voxel_grid_size[i];
+            dot = i ? dot + vs * vs : vs * vs;
+        }
+        if (!(1.1f * std::sqrt(dot) > 0.f))
+            return fail(GBT_ERR_INVALID_ARG, "voxel size too small: the truncation distance rounds to 0");
+    }
 
     gbt_volume* v = new gbt_volume();
     std::memset(v, 0, sizeof(*v));

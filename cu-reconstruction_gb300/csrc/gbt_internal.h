@@ -36,6 +36,19 @@ struct FrameDesc {
     float P[12];
 };
 
+// A frame as the integrate kernels keep it in shared memory (80 bytes, five
+// 16-byte words): pose table entry, depth image and its row pitch in elements.
+struct __align__(16) FrameSlot {
+    float pose[12];
+    const void* depth;
+    uint32_t pitch_elems;
+    float scale;
+    uint32_t width, height;
+    int32_t u16;
+    int32_t pad;
+};
+static_assert(sizeof(FrameSlot) == 80, "five 16-byte words");
+
 struct IntegrateArgs {
     VolDesc vol;
     int32_t nframes;

@@ -148,8 +148,9 @@ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, const FastDiv& f) {
 // projected corners when no corner is near the camera plane), with a margin
 // of two pixels and 1e-4 in depth that covers rounding.
 template <int MODE>
-__device__ __forceinline__ bool box_culled(const VolDesc& v, const FrameDesc& fd, const float* fr, int x_lo, int x_hi,
-                                           int y_lo, int y_hi, int z_lo, int z_hi) {
+__device__ __forceinline__ bool box_culled(const VolDesc& v, const FrameSlot& fs, int x_lo, int x_hi, int y_lo, int y_hi,
+                                           int z_lo, int z_hi) {
+    const float* fr = fs.pose;
     const float X[2] = {centre(x_lo, v.vs[0], v.off[0]), centre(x_hi, v.vs[0], v.off[0])};
     const float Y[2] = {centre(y_lo, v.vs[1], v.off[1]), centre(y_hi, v.vs[1], v.off[1])};
     const float Zw[2] = {centre(z_lo, v.vs[2], v.off[2]), centre(z_hi, v.vs[2], v.off[2])};
@@ -198,13 +199,13 @@ __device__ __forceinline__ bool box_culled(const VolDesc& v, const FrameDesc& fd
         // a box reaching behind the camera is only decided by the test above
         if (npos != 8) return false;
         // accepted pixels satisfy -0.5 <= u < width - 0.5
-        const float W = (float)fd.width, H = (float)fd.height;
+        const float W = (float)fs.width, H = (float)fs.height;
         return umax < -2.5f || umin > W + 1.5f || vmax < -2.5f || vmin > H + 1.5f;
     } else {
         if (npos != 8 && nneg != 8) return false;
         const float ccx = v.cx, ccy = v.cy;
         // truncation keeps pixel k for values in (k-1, k+1) around 0 and [k, k+1) elsewhere
-        const float W = (float)fd.width, H = (float)fd.height;
+        const float W = (float)fs.width, H = (float)fs.height;
         return umax + ccx < -3.0f || umin + ccx > W + 2.0f || vmax + ccy < -3.0f || vmin + ccy > H + 2.0f;
     }
 }
@@ -216,22 +217,32 @@ __device__ __forceinline__ bool box_culled(const VolDesc& v, const FrameDesc& fd
 // applied to the voxels in registers, in frame order, so a voxel sees exactly
 // the sequence of updates the per-frame reference loop would apply.
 
-// Per-frame pose table entry: compat -> rotation (9) + translation (3),
-// fixed -> the three rows of K[R|t].
+// A frame's shared-memory entry, written once per CTA: the pose table
+// (compat -> rotation (9) + translation (3), fixed -> the three rows of
+// K[R|t]) and the image description in the form the per-voxel code uses, so
+// that a thread reads a frame's constants with a few broadcast shared loads.
 template <int MODE>
-__device__ __forceinline__ void load_pose(const FrameDesc& fd, float* dst) {
+__device__ __forceinline__ void load_slot(const FrameDesc& fd, FrameSlot& s) {
     if (MODE == kCompat) {
         float R[9];
         compat_rotation(fd.q, R);
 #pragma unroll
-        for (int k = 0; k < 9; ++k) dst[k] = R[k];
-        dst[9] = fd.t[0];
-        dst[10] = fd.t[1];
-        dst[11] = fd.t[2];
+        for (int k = 0; k < 9; ++k) s.pose[k] = R[k];
+        s.pose[9] = fd.t[0];
+        s.pose[10] = fd.t[1];
+        s.pose[11] = fd.t[2];
     } else {
 #pragma unroll
-        for (int k = 0; k < 12; ++k) dst[k] = fd.P[k];
+        for (int k = 0; k < 12; ++k) s.pose[k] = fd.P[k];
     }
+    const bool u16 = fd.fmt == GBT_DEPTH_U16;
+    s.depth = fd.depth;
+    s.pitch_elems = (uint32_t)(u16 ? (fd.pitch >> 1) : (fd.pitch >> 2));
+    s.scale = fd.scale;
+    s.width = (uint32_t)fd.width;
+    s.height = (uint32_t)fd.height;
+    s.u16 = u16 ? 1 : 0;
+    s.pad = 0;
 }
 
 // The thread's place in a brick and its warp's sub-box.
@@ -254,16 +265,15 @@ struct BrickLayout {
 // Lane f of the warp tests frame f0 + f against the warp's sub-box; returns
 // the mask of frames that may update a voxel of it.
 template <int MODE, int TX, int BY, int BZ>
-__device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const FrameDesc* frames, const float (*pose)[12],
-                                                     int f0, int nf, const BrickLayout<TX, BY, BZ>& L, int bx0,
-                                                     int by0, int bz0) {
+__device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const FrameSlot* slots, int f0, int nf,
+                                                     const BrickLayout<TX, BY, BZ>& L, int bx0, int by0, int bz0) {
     bool live = false;
     const int f = f0 + L.lane;
     if (f < nf) {
         const int xl = bx0, xh = min(bx0 + 4 * TX, v.nx) - 1;
         const int yl = by0 + L.wy_lo, yh = min(by0 + L.wy_hi, v.ny - 1);
         const int zl = bz0 + L.wz_lo, zh = min(bz0 + L.wz_hi, v.nz - 1);
-        live = (yl <= yh && zl <= zh) && !box_culled<MODE>(v, frames[f], pose[f], xl, xh, yl, yh, zl, zh);
+        live = (yl <= yh && zl <= zh) && !box_culled<MODE>(v, slots[f], xl, xh, yl, yh, zl, zh);
     }
     return __ballot_sync(0xffffffffu, live);
 }
@@ -273,26 +283,28 @@ __device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const Fra
 // mode, lies at or in front of min_z) -- values the update skips -- and, in
 // the fixed mode, the voxel's camera z.  Split from the update so that the
 // next frame's depth gathers are in flight while this frame's running
-// averages are computed.
-template <int MODE>
-__device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc& fd, const float* pr, const float* px,
-                                              float py, float pz, int nvalid, float (&dv)[4], float (&zc)[4]) {
+// averages are computed.  FULL: the thread has all 4 voxels (nvalid == 4).
+template <int MODE, bool FULL>
+__device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot& fs, const float* px, float py, float pz,
+                                              int nvalid_, float (&dv)[4], float (&zc)[4]) {
+    const int nvalid = FULL ? 4 : nvalid_;
     // pixel (u, v) is element v * pitch_elems + u of the image (the host checks
     // that height * pitch_elems fits 32 bits and that the pitch is a whole
     // number of elements)
-    const bool u16 = fd.fmt == GBT_DEPTH_U16;
-    const unsigned short* d16 = static_cast<const unsigned short*>(fd.depth);
-    const float* d32 = static_cast<const float*>(fd.depth);
-    const uint32_t pitch_elems = (uint32_t)(u16 ? (fd.pitch >> 1) : (fd.pitch >> 2));
-    const uint32_t width = (uint32_t)fd.width, height = (uint32_t)fd.height;
+    const float* pr = fs.pose;
+    const bool u16 = fs.u16 != 0;
+    const unsigned short* d16 = static_cast<const unsigned short*>(fs.depth);
+    const float* d32 = static_cast<const float*>(fs.depth);
+    const uint32_t pitch_elems = fs.pitch_elems;
+    const uint32_t width = fs.width, height = fs.height;
     if (MODE == kCompat) {
         const float r0 = pr[0], r1 = pr[1], r2 = pr[2], r3 = pr[3], r4 = pr[4], r5 = pr[5];
         const float r6 = pr[6], r7 = pr[7], r8 = pr[8], t0 = pr[9], t1 = pr[10], t2 = pr[11];
         // world_to_pixel + camera_to_pixel (camera_util.cu:7-19,44-51) for the
-        // thread's 4 voxels, two at a time in paired FP32; a voxel with world
-        // z == 0 or camera z == 0 maps to pixel (0, 0)
+        // thread's 4 voxels, two at a time in paired FP32
         const float m0 = __fmul_rn(r1, py), m1 = __fmul_rn(r4, py), m2 = __fmul_rn(r7, py);
         int pu[4], pv[4];
+        f2 cz2[2];
 #pragma unroll
         for (int h = 0; h < 4; h += 2) {
             const f2 X = f2_pack(px[h], px[h + 1]);
@@ -301,12 +313,27 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc&
             const f2 czv = compat_cam2(r6, r8, t2, X, m2, pz);
             const f2 qu = compat_q2(cxv, v.fx, czv, v.cx);
             const f2 qv = compat_q2(cyv, v.fy, czv, v.cy);
-            const bool ok0 = pz != 0.f && f2_lo(czv) != 0.f;
-            const bool ok1 = pz != 0.f && f2_hi(czv) != 0.f;
-            pu[h] = ok0 ? (int)f2_lo(qu) : 0;
-            pv[h] = ok0 ? (int)f2_lo(qv) : 0;
-            pu[h + 1] = ok1 ? (int)f2_hi(qu) : 0;
-            pv[h + 1] = ok1 ? (int)f2_hi(qv) : 0;
+            pu[h] = (int)f2_lo(qu);
+            pv[h] = (int)f2_lo(qv);
+            pu[h + 1] = (int)f2_hi(qu);
+            pv[h + 1] = (int)f2_hi(qv);
+            cz2[h >> 1] = czv;
+        }
+        // A voxel with world z == 0 or camera z == 0 maps to pixel (0, 0).
+        // One product tests the thread's 5 z values: it is 0 or NaN whenever a
+        // factor is 0 (0 * finite = 0, 0 * inf = 0 * NaN = NaN), and a product
+        // that is 0 or NaN for any other reason (underflow, a NaN factor) only
+        // sends the thread through the per-voxel test.
+        const f2 zz = f2_mul(cz2[0], cz2[1]);
+        if (!(fabsf(__fmul_rn(__fmul_rn(f2_lo(zz), f2_hi(zz)), pz)) > 0.f)) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float cz = (i & 1) ? f2_hi(cz2[i >> 1]) : f2_lo(cz2[i >> 1]);
+                if (pz == 0.f || cz == 0.f) {
+                    pu[i] = 0;
+                    pv[i] = 0;
+                }
+            }
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -316,7 +343,7 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc&
                 const uint32_t pix = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
                 // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
                 // (rgbd_dataset.cpp:29): one float multiply
-                dv[i] = u16 ? u16_metres(__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
+                dv[i] = u16 ? u16_metres(__ldg(d16 + pix), fs.scale) : __ldg(d32 + pix);
             }
         }
     } else {
@@ -337,7 +364,7 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc&
             const int vv = __float2int_rn(__fmul_rn(V, rz));
             if ((uint32_t)u >= width || (uint32_t)vv >= height) continue;
             const uint32_t pix = (uint32_t)vv * pitch_elems + (uint32_t)u;
-            dv[i] = u16 ? __fmul_rn((float)__ldg(d16 + pix), fd.scale) : __ldg(d32 + pix);
+            dv[i] = u16 ? __fmul_rn((float)__ldg(d16 + pix), fs.scale) : __ldg(d32 + pix);
         }
 #endif
     }
@@ -345,9 +372,10 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameDesc&
 
 // One frame's running-average update of the thread's voxels from its
 // samples; returns whether any voxel changed.
-template <int MODE>
+template <int MODE, bool FULL>
 __device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)[4], const float (&zc)[4], float pz,
-                                             int nvalid, float* d, float* w, const float* s_inv) {
+                                             int nvalid_, float* d, float* w, const float* s_inv) {
+    const int nvalid = FULL ? 4 : nvalid_;
     bool dirty = false;
     if (MODE == kCompat) {
 #pragma unroll
@@ -358,8 +386,10 @@ __device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)
             if (dv[i] <= 0.0f || dv[i] > 24.0f) continue;
             const float sdf = dv[i] - pz;
             if (sdf >= -v.trunc) {
-                float tsdf = sdf;
-                if (sdf > 0) tsdf = fminf(sdf, v.trunc);
+                // the reference clamps positive values only (sdf > 0 ?
+                // min(sdf, trunc) : sdf); with trunc > 0 (the host checks it)
+                // and sdf not NaN here, min(sdf, trunc) is the same value
+                const float tsdf = fminf(sdf, v.trunc);
                 const float nw = w[i] + 1.0f;
                 const float nd = compat_avg(d[i], w[i], tsdf, nw);
                 w[i] = nw;
@@ -387,28 +417,27 @@ __device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)
     return dirty;
 }
 
-// Applies the frames of `mask` (bit f: frames[f], poses[f]) in order to the
-// thread's voxels, the next frame's samples gathered before the current
-// frame's update; returns whether any voxel changed.
-template <int MODE>
-__device__ __forceinline__ bool apply_frames(const VolDesc& v, const FrameDesc* frames, const float (*poses)[12],
-                                             uint32_t mask, int fbase, const float* px, float py, float pz,
-                                             int nvalid, float* d, float* w, const float* s_inv) {
+// Applies the frames of `mask` (bit f: slots[f]) in order to the thread's
+// voxels, the next frame's samples gathered before the current frame's
+// update; returns whether any voxel changed.
+template <int MODE, bool FULL>
+__device__ __forceinline__ bool apply_frames(const VolDesc& v, const FrameSlot* slots, uint32_t mask, const float* px,
+                                             float py, float pz, int nvalid, float* d, float* w, const float* s_inv) {
     if (!mask) return false;
     bool dirty = false;
     float dv[4], zc[4];
     int f = __ffs(mask) - 1;
     mask &= mask - 1;
-    frame_samples<MODE>(v, frames[fbase + f], poses[fbase + f], px, py, pz, nvalid, dv, zc);
+    frame_samples<MODE, FULL>(v, slots[f], px, py, pz, nvalid, dv, zc);
     for (;;) {
         float dvn[4], zcn[4];
         const bool more = mask != 0u;
         if (more) {
             f = __ffs(mask) - 1;
             mask &= mask - 1;
-            frame_samples<MODE>(v, frames[fbase + f], poses[fbase + f], px, py, pz, nvalid, dvn, zcn);
+            frame_samples<MODE, FULL>(v, slots[f], px, py, pz, nvalid, dvn, zcn);
         }
-        dirty |= frame_update<MODE>(v, dv, zc, pz, nvalid, d, w, s_inv);
+        dirty |= frame_update<MODE, FULL>(v, dv, zc, pz, nvalid, d, w, s_inv);
         if (!more) break;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -473,17 +502,31 @@ __device__ __forceinline__ void fill_inv_table(float* s_inv) {
     for (int k = threadIdx.x; k < 256; k += blockDim.x) s_inv[k] = k ? __frcp_rn((float)k) : 0.f;
 }
 
+// The frames of `mask` applied one after the other (sample, then update).
+template <int MODE, bool FULL>
+__device__ __forceinline__ bool frames_in_turn(const VolDesc& v, const FrameSlot* slots, uint32_t mask,
+                                               ThreadVoxels& t, const float* s_inv) {
+    bool dirty = false;
+    for (; mask; mask &= mask - 1) {
+        const int f = __ffs(mask) - 1;
+        float dv[4], zc[4];
+        frame_samples<MODE, FULL>(v, slots[f], t.px, t.py, t.pz, t.nvalid, dv, zc);
+        dirty |= frame_update<MODE, FULL>(v, dv, zc, t.pz, t.nvalid, t.d, t.w, s_inv);
+    }
+    return dirty;
+}
+
 template <int MODE, int TX, int BY, int BZ>
 __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ IntegrateArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
     static_assert(32 % TX == 0, "a warp spans whole x rows");
-    __shared__ float s_pose[GBT_MAX_FRAMES_PER_PASS][12];
+    __shared__ FrameSlot s_frame[GBT_MAX_FRAMES_PER_PASS];
     __shared__ float s_inv[256];
 
     const VolDesc& v = a.vol;
     const int tid = threadIdx.x;
     const int nf = a.nframes;
-    if (tid < nf) load_pose<MODE>(a.frames[tid], s_pose[tid]);
+    if (tid < nf) load_slot<MODE>(a.frames[tid], s_frame[tid]);
     if (MODE == kFixed) fill_inv_table(s_inv);
     __syncthreads();
 
@@ -497,20 +540,15 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
         const long long rest = b / nbx;
         const int bx0 = bxi * BXV, by0 = (int)(rest % nby) * BY, bz0 = (int)(rest / nby) * BZ;
         // frames for which this warp's box may contain an updated voxel
-        const uint32_t fmask = warp_live_frames<MODE>(v, a.frames, s_pose, 0, nf, L, bx0, by0, bz0);
+        const uint32_t fmask = warp_live_frames<MODE>(v, s_frame, 0, nf, L, bx0, by0, bz0);
         if (fmask == 0u) continue;
         ThreadVoxels t;
         if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
         t.load(v);
         // frame by frame (the pipelined apply_frames costs this kernel more in
         // occupancy than it gains; the batched kernel uses it)
-        bool dirty = false;
-        for (uint32_t m = fmask; m; m &= m - 1) {
-            const int f = __ffs(m) - 1;
-            float dv[4], zc[4];
-            frame_samples<MODE>(v, a.frames[f], s_pose[f], t.px, t.py, t.pz, t.nvalid, dv, zc);
-            dirty |= frame_update<MODE>(v, dv, zc, t.pz, t.nvalid, t.d, t.w, s_inv);
-        }
+        const bool dirty = t.nvalid == 4 ? frames_in_turn<MODE, true>(v, s_frame, fmask, t, s_inv)
+                                         : frames_in_turn<MODE, false>(v, s_frame, fmask, t, s_inv);
         if (dirty) t.store(v);
     }
 }
@@ -523,7 +561,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
 template <int MODE, int TX, int BY, int BZ>
 __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_constant__ BatchArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
-    __shared__ float s_pose[kBatchMaxFrames][12];
+    __shared__ FrameSlot s_frame[kBatchMaxFrames];
     __shared__ float s_inv[256];
     __shared__ long long s_task;
     __shared__ int s_scene;
@@ -554,7 +592,7 @@ __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_const
         const int nf = min(S.nframes - a.w0, a.wn);
         if (s_scene != scene) {
             scene = s_scene;
-            for (int f = tid; f < nf; f += blockDim.x) load_pose<MODE>(frames[f], s_pose[f]);
+            for (int f = tid; f < nf; f += blockDim.x) load_slot<MODE>(frames[f], s_frame[f]);
             __syncthreads();
         }
         const long long b = task - S.brick_begin;
@@ -566,18 +604,20 @@ __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_const
         bool any = false;
 #pragma unroll
         for (int c = 0; c < kBatchMaxFrames / 32; ++c) {
-            masks[c] = (c * 32 < nf) ? warp_live_frames<MODE>(v, frames, s_pose, c * 32, nf, L, bx0, by0, bz0) : 0u;
+            masks[c] = (c * 32 < nf) ? warp_live_frames<MODE>(v, s_frame, c * 32, nf, L, bx0, by0, bz0) : 0u;
             any |= masks[c] != 0u;
         }
         if (!any) continue;
         ThreadVoxels t;
         if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
         t.load(v);
+        // (a copy specialised for rows of 4 voxels, as the pass kernel has,
+        // needs 72 registers here against 64 and is slower)
         bool dirty = false;
 #pragma unroll
         for (int c = 0; c < kBatchMaxFrames / 32; ++c)
-            dirty |= apply_frames<MODE>(v, frames, s_pose, masks[c], c * 32, t.px, t.py, t.pz, t.nvalid, t.d, t.w,
-                                        s_inv);
+            dirty |= apply_frames<MODE, false>(v, s_frame + c * 32, masks[c], t.px, t.py, t.pz, t.nvalid, t.d, t.w,
+                                               s_inv);
         if (dirty) t.store(v);
     }
 }

@@ -29,6 +29,19 @@ def test_compat_ieee_bitexact_vs_oracle(gpu, oracle, case, k):
     assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
 
 
+@pytest.mark.parametrize("k", [1, 3])
+def test_compat_ieee_zero_z_voxels_vs_oracle(gpu, oracle, k):
+    """Voxels with world z == 0 or camera z == 0 read pixel (0, 0)."""
+    from test_gpu_reference import zero_z_case
+    tc, depths, poses = zero_z_case()
+    tc.arith = "ieee"
+    _, D, W = engine_run(gpu, tc, depths, poses, k=k)
+    Do, Wo = oracle_run(oracle, tc, depths, poses)
+    assert (Wo[16] == 3).all() and (Wo[20] == 3).all()
+    assert np.array_equal(W, Wo)
+    assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
+
+
 @pytest.mark.parametrize("fmt", ["u16", "f32"])
 @pytest.mark.parametrize("k", [1, 5, 32])
 @pytest.mark.parametrize("case", ["circle", "odd"])

@@ -47,6 +47,37 @@ def test_integrate_bitexact_vs_reference_kernels(gpu, ref, case, k):
     assert np.array_equal(D.view(np.uint32), Dr.view(np.uint32))
 
 
+def zero_z_case():
+    """Voxel layer 16 has world z exactly 0 and, under the identity rotation
+    with t = (., ., -0.25), layer 20 has camera z exactly 0: both map to pixel
+    (0, 0) in the reference (camera_util.cu:9,46), whose depth is 1 m."""
+    vs = 0.0625
+    n = (64, 48, 32)
+    tc = TSDFVolumeConfig(voxel_grid_size=n, physical_size=tuple(vs * k for k in n),
+                          global_offset=(-2.0, -1.5, -16.5 * vs), focal_x=100.0, focal_y=100.0, cx=31.5, cy=23.5,
+                          camera_width=64, camera_height=48)
+    rng = np.random.default_rng(7)
+    depths = []
+    for _ in range(3):
+        d = rng.uniform(0.05, 2.5, (48, 64)).astype(np.float32)
+        d[0, 0] = 1.0
+        depths.append(d)
+    poses = [np.array([1.0, 0, 0, 0, 0.0, 0.0, -0.25]), np.array([1.0, 0, 0, 0, 0.1, -0.05, -0.25]),
+             np.array([1.0, 0, 0, 0, -0.2, 0.15, -0.25])]
+    return tc, depths, poses
+
+
+@pytest.mark.parametrize("k", [1, 3])
+def test_zero_z_voxels_bitexact_vs_reference_kernels(gpu, ref, k):
+    tc, depths, poses = zero_z_case()
+    r, Dr, Wr, _ = run_reference(gpu, ref, tc, depths, poses)
+    _, D, W = engine_run(gpu, tc, depths, poses, k=k)
+    # both quirk layers were updated by every frame, through pixel (0, 0)
+    assert (Wr[16] == 3).all() and (Wr[20] == 3).all()
+    assert np.array_equal(W, Wr)
+    assert np.array_equal(D.view(np.uint32), Dr.view(np.uint32))
+
+
 def test_mesh_bitexact_vs_reference_kernels(gpu, ref):
     seq, tc = frontal_case(96, 64, 64, frames=4)
     depths = list(seq.depth_m())
