@@ -1059,10 +1059,12 @@ def main():
     alg_bytes = 16.0 * nvox + (nf / n_passes) * frame_px * 2 + (nf / n_passes) * 64
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     # DRAM bytes per launch: one ncu capture of integrate_batch_kernel at 320^3
-    # with a 64-frame window read and wrote 274.0 + 168.4 MB (bricks no frame
-    # sees are not loaded, unchanged ones not stored), i.e. 13.50 B per voxel;
-    # scaled by voxels for the same window.  Other configurations: not measured.
-    traffic = 442.45e6 / 320 ** 3 * nvox if (path == "batched" and K == 64 and args.mode == "compat") else None
+    # with a 64-frame window of 640x480 uint16 images read and wrote 274.4 +
+    # 168.2 MB (bricks no frame sees are not loaded, unchanged ones not
+    # stored).  Less the window's images read once (64 x 614.4 KB) that is
+    # 12.31 B per voxel; scaled by voxels, plus this launch's images.  The
+    # pass kernel and the fixed mode: not captured.
+    traffic = (12.31 * nvox + (nf / n_passes) * frame_px * 2) if (path == "batched" and args.mode == "compat") else None
     peak, peak_kind = peaks()
 
     # end to end through the public API with host buffers: H2D of the step's

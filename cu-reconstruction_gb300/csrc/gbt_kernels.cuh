@@ -98,11 +98,16 @@ __device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) 
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(cz));
     return __fmaf_rn(__fmul_rn(c, f), r, cc);
 }
-__device__ __forceinline__ f2 compat_q2(f2 c, float f, f2 cz, float cc) {
+// Pixel coordinates (u, v) of two voxels from their camera coordinates; the
+// reciprocal of each z serves both.
+__device__ __forceinline__ void compat_proj2(f2 cx, f2 cy, f2 cz, float fx, float fy, float ccx, float ccy, f2& qu,
+                                             f2& qv) {
     float r0, r1;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(f2_lo(cz)));
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(f2_hi(cz)));
-    return f2_fma(f2_mul(c, f2_splat(f)), f2_pack(r0, r1), f2_splat(cc));
+    const f2 r = f2_pack(r0, r1);
+    qu = f2_fma(f2_mul(cx, f2_splat(fx)), r, f2_splat(ccx));
+    qv = f2_fma(f2_mul(cy, f2_splat(fy)), r, f2_splat(ccy));
 }
 __device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
     return ((d * w) + (tsdf * 1.0f)) / nw;
@@ -121,6 +126,11 @@ __device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) 
 __device__ __forceinline__ f2 compat_q2(f2 c, float f, f2 cz, float cc) {
     const f2 m = f2_mul(c, f2_splat(f));
     return f2_add(f2_pack(__fdiv_rn(f2_lo(m), f2_lo(cz)), __fdiv_rn(f2_hi(m), f2_hi(cz))), f2_splat(cc));
+}
+__device__ __forceinline__ void compat_proj2(f2 cx, f2 cy, f2 cz, float fx, float fy, float ccx, float ccy, f2& qu,
+                                             f2& qv) {
+    qu = compat_q2(cx, fx, cz, ccx);
+    qv = compat_q2(cy, fy, cz, ccy);
 }
 __device__ __forceinline__ float compat_avg(float d, float w, float tsdf, float nw) {
     return __fdiv_rn(__fmaf_rn(d, w, tsdf), nw);
@@ -311,8 +321,8 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
             const f2 cxv = compat_cam2(r0, r2, t0, X, m0, pz);
             const f2 cyv = compat_cam2(r3, r5, t1, X, m1, pz);
             const f2 czv = compat_cam2(r6, r8, t2, X, m2, pz);
-            const f2 qu = compat_q2(cxv, v.fx, czv, v.cx);
-            const f2 qv = compat_q2(cyv, v.fy, czv, v.cy);
+            f2 qu, qv;
+            compat_proj2(cxv, cyv, czv, v.fx, v.fy, v.cx, v.cy, qu, qv);
             pu[h] = (int)f2_lo(qu);
             pv[h] = (int)f2_lo(qv);
             pu[h + 1] = (int)f2_hi(qu);
@@ -335,16 +345,23 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
                 }
             }
         }
+        // tsdf_volume.cu:166-170 (negative u, v wrap to large unsigned values)
+        bool in[4];
+        uint32_t pix[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            dv[i] = 0.f;
-            // tsdf_volume.cu:166-170 (negative u, v wrap to large unsigned values)
-            if (i < nvalid && (uint32_t)pu[i] < width && (uint32_t)pv[i] < height) {
-                const uint32_t pix = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
-                // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
-                // (rgbd_dataset.cpp:29): one float multiply
-                dv[i] = u16 ? u16_metres(__ldg(d16 + pix), fs.scale) : __ldg(d32 + pix);
-            }
+            in[i] = i < nvalid && (uint32_t)pu[i] < width && (uint32_t)pv[i] < height;
+            pix[i] = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
+        }
+        // the format is the same for every thread of the CTA: one gather loop each
+        if (u16) {
+            // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
+            // (rgbd_dataset.cpp:29): one float multiply
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? u16_metres(__ldg(d16 + pix[i]), fs.scale) : 0.f;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? __ldg(d32 + pix[i]) : 0.f;
         }
     } else {
 #if !defined(GBT_REF_ARITH)
@@ -1133,6 +1150,31 @@ cudaError_t launch_batch_mode(const BatchArgs& a, int brick, int grid, cudaStrea
         case 2: return launch_batch_shape<MODE, 8, 2, 8>(a, grid, s);
         case 3: return launch_batch_shape<MODE, 16, 2, 4>(a, grid, s);
         default: return launch_batch_shape<MODE, 8, 4, 4>(a, grid, s);
+    }
+}
+
+// CTAs of an integrate kernel that fit on one SM at once (registers and
+// shared memory decide it); the default persistent grid is SMs times this.
+template <typename Kernel>
+int resident_128(Kernel k) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, 0) != cudaSuccess) cudaGetLastError();
+    return n > 0 ? n : 1;
+}
+
+template <int MODE, int TX, int BY, int BZ>
+int resident_shape(bool batched) {
+    return batched ? resident_128(integrate_batch_kernel<MODE, TX, BY, BZ>)
+                   : resident_128(integrate_kernel<MODE, TX, BY, BZ>);
+}
+
+template <int MODE>
+int resident_ctas_mode(bool batched, int brick) {
+    switch (brick) {
+        case 1: return resident_shape<MODE, 4, 8, 4>(batched);
+        case 2: return resident_shape<MODE, 8, 2, 8>(batched);
+        case 3: return resident_shape<MODE, 16, 2, 4>(batched);
+        default: return resident_shape<MODE, 8, 4, 4>(batched);
     }
 }
 

@@ -24,6 +24,10 @@ cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStre
     return launch_batch_mode<kFixed>(a, brick, grid, s);
 }
 
+int integrate_resident_ctas_compat_ieee(bool batched, int brick) { return resident_ctas_mode<kCompat>(batched, brick); }
+
+int integrate_resident_ctas_fixed(bool batched, int brick) { return resident_ctas_mode<kFixed>(batched, brick); }
+
 cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kCompat>(a, s); }
 
 cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kFixed>(a, s); }

@@ -3,7 +3,7 @@
 Each candidate integrates the same frames into the volume (which is reset
 before and after), timed with CUDA events on the launching stream; the
 fastest is kept.  Results are cached per (GPU, grid, image size, mode,
-arithmetic) in a JSON file next to the engine library.
+arithmetic, build of the engine library) in a JSON file next to the library.
 """
 import json
 import os
@@ -12,15 +12,20 @@ from . import _lib as L
 
 BRICKS = (0, 1, 2, 3)
 FRAMES = (8, 16, 32)
-CTAS = (4, 8, 12, 16)
+CTAS = (0, 4, 8, 16)   # 0: as many as the kernel keeps resident
 CACHE = os.path.join(L.PKG_ROOT, "_build", "autotune.json")
 
 
 def _key(vol, width, height):
     import torch
     c = vol.cfg
-    return "%s|%s|%dx%d|%s|%s" % (torch.cuda.get_device_name(), "x".join(map(str, c.voxel_grid_size)), width, height,
-                                  c.mode, c.arith)
+    try:
+        st = os.stat(L.LIB_PATH)
+        build = "%d-%d" % (st.st_size, st.st_mtime_ns)
+    except OSError:
+        build = "?"
+    return "%s|%s|%dx%d|%s|%s|%s" % (torch.cuda.get_device_name(), "x".join(map(str, c.voxel_grid_size)), width,
+                                     height, c.mode, c.arith, build)
 
 
 def _load():
@@ -88,7 +93,7 @@ def tune_integrate(vol, depths, poses, depth_scale=0.001, bricks=BRICKS, frames=
 WINDOWS = (32, 64, 128)
 
 
-def tune_batched(vol, depths, poses, batch, depth_scale=0.001, bricks=(0, 1, 2, 3), windows=WINDOWS, ctas=(8, 16),
+def tune_batched(vol, depths, poses, batch, depth_scale=0.001, bricks=(0, 1, 2, 3), windows=WINDOWS, ctas=(0, 16),
                  repeats=2, use_cache=True):
     """The same search for the batched path (gbt_integrate_batch with this one
     volume): brick shape x frames per launch window x CTAs per SM, timed on
