@@ -51,7 +51,8 @@ struct gbt_volume {
     int64_t nvox;
     bool managed;
     void* tvox;
-    // marching-cubes scratch: [0,64) header (ticket u32, error i32, total i64), then status words
+    // marching-cubes scratch: [0,64) header (ticket u32, error i32, total i64, tiles listed u32),
+    // then one u64 word per tile, then the u32 list of tiles with triangles
     void* mc_scratch;
     size_t mc_scratch_bytes;
     // shared-vertex mesh scratch: used-edge bits, word offsets, block sums, vertex count
@@ -389,7 +390,7 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     a->tris = tris;
     a->cap = cap;
     a->index_base = index_base;
-    const size_t need = 64 + (size_t)a->ntiles * 8;
+    const size_t need = 64 + (size_t)a->ntiles * 12;
     if (v->mc_scratch_bytes < need) {
         if (v->mc_scratch) cudaFree(v->mc_scratch);
         v->mc_scratch = nullptr;
@@ -405,7 +406,9 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     a->ticket = reinterpret_cast<unsigned int*>(s);
     a->error = reinterpret_cast<int*>(s + 4);
     a->total = reinterpret_cast<long long*>(s + 8);
+    a->nonempty = reinterpret_cast<unsigned int*>(s + 16);
     a->status = reinterpret_cast<unsigned long long*>(s + 64);
+    a->tile_list = reinterpret_cast<uint32_t*>(s + 64 + (size_t)a->ntiles * 8);
     return GBT_OK;
 }
 
@@ -446,7 +449,7 @@ gbt_status gbt_extract_mesh(gbt_volume* v, float* verts, int32_t* tris, int64_t 
     cudaError_t e = cudaMemcpyAsync(&hdr, v->mc_scratch, sizeof(hdr), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh extraction");
-    if (hdr.error) return fail(GBT_ERR_TIMEOUT, "mesh extraction: a tile gave up waiting for its predecessor");
+    if (hdr.error) return fail(GBT_ERR_CUDA, "mesh extraction: the kernels set their error word");
     *n_tris = hdr.total;
     if (hdr.total > cap_tris && cap_tris > 0)
         return fail(GBT_ERR_CAPACITY, "mesh has %lld triangles, buffer holds %lld", hdr.total, (long long)cap_tris);
@@ -827,7 +830,7 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* v, float* verts, float* normals,
     e = cudaMemcpyAsync(&hdr, v->mc_scratch, sizeof(hdr), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh extraction");
-    if (hdr.error) return fail(GBT_ERR_TIMEOUT, "mesh extraction: a tile gave up waiting for its predecessor");
+    if (hdr.error) return fail(GBT_ERR_CUDA, "mesh extraction: the kernels set their error word");
     *n_tris = hdr.total;
     if ((hdr.total > cap_tris && cap_tris > 0) || (nv > cap_verts && cap_verts > 0))
         return fail(GBT_ERR_CAPACITY, "mesh has %lld vertices and %lld triangles, buffers hold %lld and %lld", nv,

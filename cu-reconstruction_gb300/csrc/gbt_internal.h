@@ -102,8 +102,9 @@ inline FastDiv make_fastdiv(uint32_t d) {
     return f;
 }
 
-// Marching cubes over the linear cube order (z, y, x), one tile of
-// mc_tile_cubes(mode) cubes per CTA and tile, tiles chained by a decoupled look-back.
+// Marching cubes over the linear cube order (z, y, x) in tiles of
+// mc_tile_cubes(mode) cubes: counted per tile, offsets by a scan of the tile
+// counts, then one CTA per tile with triangles emits them.
 constexpr int kMcThreads = 256;
 // Cubes per thread per tile: 8 in the compat mode (one D load per corner), 4
 // in the fixed mode (which also loads W, and keeps twice the values in flight).
@@ -128,10 +129,12 @@ struct McArgs {
     int32_t* tris;
     int64_t cap;
     int64_t index_base;
-    unsigned long long* status;  // [ntiles] look-back words, zeroed before launch
-    unsigned int* ticket;        // tile ticket, zeroed before launch
+    unsigned long long* status;  // [ntiles] triangles per tile, then exclusive offsets; zeroed before launch
+    uint32_t* tile_list;         // [ntiles] tiles with triangles, in order
+    unsigned int* nonempty;      // length of tile_list
+    unsigned int* ticket;        // emission ticket, zeroed before launch
     long long* total;            // triangle count out
-    int* error;                  // set to 1 when a look-back wait gives up
+    int* error;                  // stays 0: no launch waits on another CTA
     // Fixed mode with shared vertices: when edge_bits is set, triangles are
     // written as indices of the vertices of their grid edges (edge
     // 3 * voxel + axis; vertex index = edge_word_offset[edge / 32] + the set

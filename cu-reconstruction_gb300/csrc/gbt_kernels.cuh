@@ -646,20 +646,6 @@ __device__ __forceinline__ int corner_dx(int k) { return (0x66 >> k) & 1; }
 __device__ __forceinline__ int corner_dy(int k) { return (0xF0 >> k) & 1; }
 __device__ __forceinline__ int corner_dz(int k) { return (0xCC >> k) & 1; }
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-constexpr unsigned long long kFlagAgg = 1ull << 62;
-constexpr unsigned long long kFlagIncl = 2ull << 62;
-constexpr unsigned long long kValueMask = (1ull << 62) - 1;
-constexpr int kLookbackSpinLimit = 1 << 22;
-
 // Linear index of corner 0 of cube (cx, cy, cz) and of the next layer.
 template <int MODE>
 __device__ __forceinline__ void cube_base(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int64_t* b0,
@@ -684,55 +670,219 @@ __device__ __forceinline__ int64_t weld_edge_id(const McArgs& a, uint32_t cx, ui
     return 3 * lin + axis;
 }
 
-// Cube types (the 8-bit corner sign pattern, 0 for a cube that is not
-// emitted) of cubes i0 .. i0+3 of the thread's cubes in a tile.  Every corner
-// load of the batch is issued before any is used; a cube past the end reads
-// the last cube, in bounds, and is discarded.
-template <int MODE, int CPT>
-__device__ __forceinline__ void mc_classify4(const McArgs& a, uint32_t tile, int tid, int i0, int (&type)[CPT]) {
-    const uint32_t c0 = tile * (uint32_t)(kMcThreads * CPT);
-    float dv[4][8];
-    float wv[4][8];
+// Cube classification by warps.  The 32 lanes of a warp take 32 consecutive
+// cubes (linear order).  A lane loads the corners of its cube at x (corners
+// 0, 3, 4 and 7: (y, z), (y, z+1), (y+1, z), (y+1, z+1)) and packs their signs
+// into a nibble, with, in the fixed mode, a fifth bit for "all four weights
+// > 0"; the corners at x + 1 are the next lane's corners at x, so one shuffle
+// of the nibble completes the cube, except for lane 31 and for the last cube
+// of a grid row, which load their x + 1 corners themselves (those loads are
+// issued with the others, predicated).  A table maps the (own, next) nibble
+// pair to the 8-bit type in the reference's corner numbering.
+__device__ __forceinline__ int mc_type_of_nibbles(int sx, int sn) {
+    return (sx & 1) | (sn & 1) << 1 | ((sn >> 1) & 1) << 2 | ((sx >> 1) & 1) << 3 | ((sx >> 2) & 1) << 4 |
+           ((sn >> 2) & 1) << 5 | ((sn >> 3) & 1) << 6 | ((sx >> 3) & 1) << 7;
+}
+
+// Linear indices of corners 0, 3, 4, 7 of cube c and whether its x + 1
+// corners are the next cube's x corners (not so at the end of a row).  All
+// indices are below 2^32: the host limits volumes to 2^32 - 1 voxels, and the
+// compat layer stride (gx + gy) stays within the grid.
+template <int MODE>
+__device__ __forceinline__ bool cube_xcorners(const McArgs& a, uint32_t c, uint32_t (&idx)[4]) {
+    const uint32_t row = fastdiv(c, a.div_cx);
+    const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
+    const uint32_t cz = fastdiv(row, a.div_cy);
+    const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+    const uint32_t gx = (uint32_t)a.gx;
+    const uint32_t layer = (MODE == kCompat) ? gx + (uint32_t)a.gy : gx * (uint32_t)a.gy;   // marching_cubes.cu:211
+    const uint32_t b0 = cz * layer + cy * gx + cx, b1 = b0 + layer;
+    idx[0] = b0;
+    idx[1] = b1;
+    idx[2] = b0 + gx;
+    idx[3] = b1 + gx;
+    return cx + 2 == gx;
+}
+
+// Types (0 for a cube that is not emitted: past the end, or in the fixed mode
+// with a corner of weight <= 0) of the lane's cubes cube[0..NB) -- each lane
+// of the warp holding the cube after the previous lane's -- with every load
+// of the NB cubes issued before any is used.  A cube past the end reads the
+// last cube, in bounds, and is discarded.
+template <int MODE, int NB>
+__device__ __forceinline__ void mc_types(const McArgs& a, const uint64_t (&cube)[NB], int lane, int (&type)[NB],
+                                         const unsigned char* s_type) {
+    float dx[NB][4], dn[NB][4];
+    float wx[NB][4], wn[NB][4];
+    bool own[NB];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        uint32_t c = c0 + (i0 + i) * kMcThreads + tid;
-        c = c < a.ncubes ? c : a.ncubes - 1;
-        const uint32_t row = fastdiv(c, a.div_cx);
-        const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
-        const uint32_t cz = fastdiv(row, a.div_cy);
-        const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
-        int64_t b0, b1;
-        cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+    for (int i = 0; i < NB; ++i) {
+        const uint32_t c = cube[i] < a.ncubes ? (uint32_t)cube[i] : a.ncubes - 1;
+        uint32_t idx[4];
+        own[i] = cube_xcorners<MODE>(a, c, idx) || lane == 31;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int64_t idx = corner_index<MODE>(a, b0, b1, k);
-            dv[i][k] = __ldg(a.D + idx);
-            if (MODE == kFixed) wv[i][k] = __ldg(a.W + idx);
+        for (int k = 0; k < 4; ++k) {
+            dx[i][k] = __ldg(a.D + idx[k]);
+            dn[i][k] = own[i] ? __ldg(a.D + idx[k] + 1) : 0.f;
+            if (MODE == kFixed) {
+                wx[i][k] = __ldg(a.W + idx[k]);
+                wn[i][k] = own[i] ? __ldg(a.W + idx[k] + 1) : 0.f;
+            }
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        int t = 0;
-        bool ok = c0 + (i0 + i) * kMcThreads + tid < a.ncubes;
+    for (int i = 0; i < NB; ++i) {
+        int sx = 0, so = 0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            if (dv[i][k] < 0.f) t |= 1 << k;
-            if (MODE == kFixed) ok &= wv[i][k] > 0.f;
+        for (int k = 0; k < 4; ++k) {
+            sx |= (dx[i][k] < 0.f) << k;
+            so |= (dn[i][k] < 0.f) << k;
         }
-        type[i0 + i] = ok ? t : 0;
+        if (MODE == kFixed) {
+            const bool okx = wx[i][0] > 0.f && wx[i][1] > 0.f && wx[i][2] > 0.f && wx[i][3] > 0.f;
+            const bool oko = wn[i][0] > 0.f && wn[i][1] > 0.f && wn[i][2] > 0.f && wn[i][3] > 0.f;
+            sx |= okx << 4;
+            so |= oko << 4;
+        }
+        // every lane takes part in the shuffle; a lane then keeps its own loads or the next lane's
+        const int nx = __shfl_down_sync(0xffffffffu, sx, 1);
+        const int sn = own[i] ? so : nx;
+        const int t = s_type[(sx & 15) | (sn & 15) << 4];
+        bool ok = cube[i] < a.ncubes;
+        if (MODE == kFixed) ok = ok && (sx & sn & 16);
+        type[i] = ok ? t : 0;
     }
 }
 
-// Single-pass marching cubes over tiles of mc_tile_cubes(MODE) cubes taken by ticket.
-// Per tile: classify (corner loads batched four cubes at a time), warp scans
-// of the triangle counts, warp 0 scans the partial sums and looks back over
-// the preceding tiles for the tile's offset, then every thread emits its
-// cubes' triangles straight to their final positions.
+// Types of the thread's cubes of a tile: cube c0 + i * kMcThreads + tid for
+// i < CPT, NB of them at a time (the fixed mode also loads weights: half as
+// many in flight).
+template <int MODE, int CPT>
+__device__ __forceinline__ void mc_tile_types(const McArgs& a, uint32_t tile, int tid, int (&type)[CPT],
+                                              const unsigned char* s_type) {
+    constexpr int NB = MODE == kFixed ? 2 : 4;
+    const uint64_t c0 = (uint64_t)tile * (kMcThreads * CPT);
+#pragma unroll
+    for (int i0 = 0; i0 < CPT; i0 += NB) {
+        uint64_t cube[NB];
+        int t[NB];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) cube[i] = c0 + (uint64_t)(i0 + i) * kMcThreads + tid;
+        mc_types<MODE, NB>(a, cube, tid & 31, t, s_type);
+#pragma unroll
+        for (int i = 0; i < NB; ++i) type[i0 + i] = t[i];
+    }
+}
+
+__device__ __forceinline__ void mc_load_tables(unsigned char* s_count, unsigned long long* s_tri, unsigned char* s_ends,
+                                               unsigned char* s_type) {
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+        if (s_count) s_count[k] = GBT_MC_TRI_COUNT[k];
+        if (s_tri) s_tri[k] = GBT_MC_TRI_PACKED[k];
+        s_type[k] = (unsigned char)mc_type_of_nibbles(k & 15, k >> 4);
+    }
+    if (s_ends && threadIdx.x < 12) s_ends[threadIdx.x] = GBT_MC_EDGE_ENDS[threadIdx.x];
+}
+
+// Marching cubes in three launches, none of which waits on another CTA.
+// (1) mc_count_kernel: warps classify groups of 32 consecutive cubes and add
+//     each group's triangle count to its tile's word (tiles of
+//     mc_tile_cubes(MODE) cubes in linear cube order; the words start at 0).
+// (2) mc_scan_kernel: one CTA turns the tile counts into exclusive offsets in
+//     place, lists the tiles that have triangles, and writes the total.
+// (3) mc_emit_kernel: CTAs take listed tiles by ticket, classify the tile
+//     again, scan its counts and write its triangles from the tile's offset.
+// Triangles come out in the reference's linear cube order.
 template <int MODE>
-__global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McArgs a) {
+__global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_constant__ McArgs a) {
+    __shared__ unsigned char s_count[256];
+    __shared__ unsigned char s_type[256];
+    mc_load_tables(s_count, nullptr, nullptr, s_type);
+    __syncthreads();
+    constexpr uint64_t kTile = mc_tile_cubes(MODE);
+    constexpr int NB = MODE == kFixed ? 2 : 4;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t ngroups = ((uint64_t)a.ncubes + 31) / 32;
+    // the loop bound is the same for all lanes of a warp
+    for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += NB * nwarps) {
+        uint64_t cube[NB];
+        int t[NB];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) cube[i] = (g + i * nwarps) * 32 + lane;
+        mc_types<MODE, NB>(a, cube, lane, t, s_type);
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            const unsigned n = __reduce_add_sync(0xffffffffu, (unsigned)s_count[t[i]]);
+            const uint64_t gi = g + i * nwarps;
+            if (lane == 0 && n != 0u && gi < ngroups) atomicAdd(a.status + gi * 32 / kTile, (unsigned long long)n);
+        }
+    }
+}
+
+constexpr int kMcScanThreads = 1024;
+
+// Exclusive offsets of the tiles (in place), the list of tiles with
+// triangles, the triangle total and the list length.  A thread takes a
+// contiguous run of tiles; its sums travel packed as (triangles << 24 |
+// tiles with triangles): at most 5 * 2^32 triangles and 2^22 tiles, so
+// neither field carries into the other.
+__global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_constant__ McArgs a) {
+    __shared__ unsigned long long s_part[kMcScanThreads / 32];
+    const uint32_t n = a.ntiles;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t per = (n + kMcScanThreads - 1) / kMcScanThreads;
+    const uint32_t b = min(tid * per, n), e = min(b + per, n);
+    unsigned long long own = 0;
+#pragma unroll 8
+    for (uint32_t i = b; i < e; ++i) {
+        const unsigned long long c = a.status[i];
+        own += (c << 24) | (c != 0ull ? 1ull : 0ull);
+    }
+    unsigned long long x = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_part[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const unsigned long long v = s_part[lane];
+        unsigned long long p = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, p, o);
+            if (lane >= (uint32_t)o) p += y;
+        }
+        s_part[lane] = p - v;
+    }
+    __syncthreads();
+    const unsigned long long excl = s_part[warp] + x - own;
+    unsigned long long off = excl >> 24;
+    uint32_t k = (uint32_t)(excl & 0xffffffull);
+    for (uint32_t i = b; i < e; ++i) {
+        const unsigned long long c = a.status[i];
+        a.status[i] = off;
+        if (c) a.tile_list[k++] = i;
+        off += c;
+    }
+    if (tid == kMcScanThreads - 1) {
+        const unsigned long long all = excl + own;
+        *a.total = (long long)(all >> 24);
+        *a.nonempty = (unsigned)(all & 0xffffffull);
+    }
+}
+
+// Emission: a CTA takes the next listed tile, classifies its cubes, scans
+// the triangle counts (warp scans, then warp 0 over the partial sums) and
+// writes every cube's triangles from the tile's offset.
+template <int MODE>
+__global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_constant__ McArgs a) {
     __shared__ unsigned char s_count[256];
     __shared__ unsigned long long s_tri[256];
     __shared__ unsigned char s_ends[12];
+    __shared__ unsigned char s_type[256];
     constexpr int kWarps = kMcThreads / 32;
     constexpr int CPT = mc_cubes_per_thread(MODE);
     constexpr int kTile = kMcThreads * CPT;
@@ -740,29 +890,26 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
     static_assert(kParts % 32 == 0 && kParts <= 32 * 4, "warp 0 scans the partial sums, up to 4 per lane");
     constexpr int kPerLane = kParts / 32;
     __shared__ int s_wsum[kParts];
-    __shared__ unsigned int s_tile;
-    __shared__ long long s_prefix;
+    __shared__ unsigned int s_job;
 
     const int tid = threadIdx.x;
-    for (int k = tid; k < 256; k += kMcThreads) {
-        s_count[k] = GBT_MC_TRI_COUNT[k];
-        s_tri[k] = GBT_MC_TRI_PACKED[k];
-    }
-    if (tid < 12) s_ends[tid] = GBT_MC_EDGE_ENDS[tid];
+    mc_load_tables(s_count, s_tri, s_ends, s_type);
     const int lane = tid & 31, warp = tid >> 5;
+    const unsigned njobs = *a.nonempty;
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+        if (tid == 0) s_job = atomicAdd(a.ticket, 1u);
         __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= a.ntiles) return;
+        const unsigned job = s_job;
+        if (job >= njobs) return;
+        const uint32_t tile = a.tile_list[job];
+        const long long tile_prefix = (long long)a.status[tile];
         const uint32_t c0 = tile * (uint32_t)kTile;
 
         int type[CPT];
         int incl[CPT];
-#pragma unroll
-        for (int i0 = 0; i0 < CPT; i0 += 4) mc_classify4<MODE, CPT>(a, tile, tid, i0, type);
+        mc_tile_types<MODE, CPT>(a, tile, tid, type, s_type);
 #pragma unroll
         for (int i = 0; i < CPT; ++i) {
             int n = s_count[type[i]];
@@ -791,59 +938,14 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
                 const int y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
-            const int total = __shfl_sync(0xffffffffu, x, 31);
             int run = x - local;
 #pragma unroll
             for (int q = 0; q < kPerLane; ++q) {
                 s_wsum[lane * kPerLane + q] = run;
                 run += v[q];
             }
-            // decoupled look-back over the preceding tiles, 32 at a time: lane
-            // l reads tile (j - l); the nearest tile with an inclusive prefix
-            // ends the walk, the aggregates before it are summed by the warp
-            long long prefix = 0;
-            if (tile == 0) {
-                if (lane == 0) st_release(a.status + tile, kFlagIncl | (unsigned long long)total);
-            } else {
-                if (lane == 0) st_release(a.status + tile, kFlagAgg | (unsigned long long)total);
-                int64_t j = (int64_t)tile - 1;
-                int spins = 0;
-                bool failed = false;
-                while (j >= 0) {
-                    const int64_t mine = j - lane;
-                    unsigned long long w = mine >= 0 ? ld_acquire(a.status + mine) : kFlagIncl;
-                    // wait until every tile of the window has published something
-                    while (__any_sync(0xffffffffu, (w & ~kValueMask) == 0ull)) {
-                        if (++spins > kLookbackSpinLimit) {
-                            failed = true;
-                            break;
-                        }
-                        __nanosleep(64);
-                        if ((w & ~kValueMask) == 0ull) w = ld_acquire(a.status + mine);
-                    }
-                    if (failed) break;
-                    const unsigned incl_lanes = __ballot_sync(0xffffffffu, (w & ~kValueMask) == kFlagIncl);
-                    const int stop = incl_lanes ? __ffs(incl_lanes) - 1 : 31;   // nearest inclusive tile
-                    long long sv = lane <= stop ? (long long)(w & kValueMask) : 0;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
-                    prefix += sv;
-                    if (incl_lanes) break;
-                    j -= 32;
-                }
-                if (failed) {
-                    if (lane == 0) atomicExch(a.error, 1);
-                } else if (lane == 0) {
-                    st_release(a.status + tile, kFlagIncl | (unsigned long long)(prefix + total));
-                }
-            }
-            if (lane == 0) {
-                s_prefix = prefix;
-                if (tile == a.ntiles - 1) *a.total = prefix + total;
-            }
         }
         __syncthreads();
-        const long long tile_prefix = s_prefix;
 
 #pragma unroll
         for (int i = 0; i < CPT; ++i) {
@@ -929,37 +1031,53 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
 // triangles use; (2) weld_count / weld_scan_blocks / weld_offsets: an
 // exclusive scan of the bit counts numbers the used edges (vertex index =
 // word offset + set bits below); (3) weld_vertices: one vertex per used
-// edge, interpolated exactly as mc_kernel<kFixed> interpolates it (lower
+// edge, interpolated exactly as mc_emit_kernel<kFixed> interpolates it (lower
 // endpoint first, so the positions are the ones the triangle soup holds),
 // with the normal of the interpolated central-difference gradient;
-// (4) mc_kernel<kFixed> with edge_bits set writes the triangles as indices,
+// (4) mc_emit_kernel<kFixed> with edge_bits set writes the triangles as indices,
 // in the same order as the triangle soup.
 __global__ void __launch_bounds__(256) weld_mark_kernel(const __grid_constant__ McArgs a, uint32_t* bits) {
     __shared__ unsigned char s_count[256];
     __shared__ unsigned long long s_tri[256];
     __shared__ unsigned char s_ends[12];
+    __shared__ unsigned char s_type[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) {
         s_count[k] = GBT_MC_TRI_COUNT[k];
         s_tri[k] = GBT_MC_TRI_PACKED[k];
+        s_type[k] = (unsigned char)mc_type_of_nibbles(k & 15, k >> 4);
     }
     if (threadIdx.x < 12) s_ends[threadIdx.x] = GBT_MC_EDGE_ENDS[threadIdx.x];
     __syncthreads();
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncubes; c += gridDim.x * blockDim.x) {
+    // whole warps take 32 consecutive cubes (the classification shuffles)
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < a.ncubes; w0 += stride) {
+        const bool valid = w0 + lane < a.ncubes;
+        const uint32_t c = valid ? (uint32_t)(w0 + lane) : a.ncubes - 1;
+        uint32_t idx[4];
+        const bool own = cube_xcorners<kFixed>(a, c, idx) || lane == 31;
+        int sx = 0, so = 0;
+        bool okx = true, oko = true;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            sx |= (__ldg(a.D + idx[k]) < 0.f) << k;
+            okx = okx && __ldg(a.W + idx[k]) > 0.f;
+            if (own) {
+                so |= (__ldg(a.D + idx[k] + 1) < 0.f) << k;
+                oko = oko && __ldg(a.W + idx[k] + 1) > 0.f;
+            }
+        }
+        sx |= okx << 4;
+        so |= oko << 4;
+        // every lane takes part in the shuffle; a lane then keeps its own loads or the next lane's
+        const int nx = __shfl_down_sync(0xffffffffu, sx, 1);
+        const int sn = own ? so : nx;
+        if (!valid || !(sx & sn & 16)) continue;
+        const int t = s_type[(sx & 15) | (sn & 15) << 4];
         const uint32_t row = fastdiv(c, a.div_cx);
         const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
         const uint32_t cz = fastdiv(row, a.div_cy);
         const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
-        int64_t b0, b1;
-        cube_base<kFixed>(a, cx, cy, cz, &b0, &b1);
-        int t = 0;
-        bool ok = true;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int64_t idx = corner_index<kFixed>(a, b0, b1, k);
-            ok &= __ldg(a.W + idx) > 0.f;
-            if (__ldg(a.D + idx) < 0.f) t |= 1 << k;
-        }
-        if (!ok) continue;
         const int n = s_count[t];
         const unsigned long long edges = s_tri[t];
         for (int q = 0; q < 3 * n; ++q) {
@@ -1178,20 +1296,31 @@ int resident_ctas_mode(bool batched, int brick) {
     }
 }
 
+// The three marching-cubes launches; the scratch words (ticket, total, list
+// length, tile words) are zero when the first starts.
 template <int MODE>
 cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
-    static int sms = 0, per_sm = 0;
+    static int sms = 0, per_count = 0, per_emit = 0;
     if (sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<MODE>, kMcThreads, 0);
-        if (per_sm < 1) per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_count, mc_count_kernel<MODE>, kMcThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_emit, mc_emit_kernel<MODE>, kMcThreads, 0);
+        if (per_count < 1) per_count = 1;
+        if (per_emit < 1) per_emit = 1;
     }
-    long long grid = (long long)sms * per_sm;
+    const long long groups_per_cta = kMcThreads / 32 * (MODE == kFixed ? 2 : 4);
+    long long grid = (long long)sms * per_count;
+    const long long need = ((long long)a.ncubes + 32 * groups_per_cta - 1) / (32 * groups_per_cta);
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
+    mc_scan_kernel<<<1, kMcScanThreads, 0, s>>>(a);
+    grid = (long long)sms * per_emit;
     if (grid > (long long)a.ntiles) grid = a.ntiles;
     if (grid < 1) grid = 1;
-    mc_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
+    mc_emit_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -1,6 +1,6 @@
 // Mesh extraction that allocates no device memory.
 //
-// gbt_extract_mesh lets the engine cudaMalloc its look-back scratch the first
+// gbt_extract_mesh lets the engine cudaMalloc its tile scratch the first
 // time a volume is meshed.  Some callers cannot allow that: code that runs
 // while a CUDA graph is being captured in the global capture mode (where
 // cudaMalloc is an error), and applications that hand all device memory to
@@ -19,8 +19,9 @@
 
 namespace {
 
-// [0, 64): tile ticket (u32), look-back error flag (i32), triangle total (i64);
-// then one look-back status word (u64) per tile (at least 1024 cubes).
+// [0, 64): emission ticket (u32), error flag (i32), triangle total (i64),
+// tiles listed (u32); then one word (u64) per tile (at least 1024 cubes) and
+// the list of tiles with triangles (u32 per tile).
 static __device__ __align__(256) unsigned char g_mesh_scratch[GBT_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
@@ -45,7 +46,7 @@ cudaError_t scratch_address(void** out) {
     return cudaSuccess;
 }
 
-// Count for the caller: the total, or -1 when a look-back wait gave up.
+// Count for the caller: the total, or -1 if the kernels set their error word.
 __global__ void finish_count(const unsigned char* scratch, int64_t* d_n_tris) {
     const int err = *reinterpret_cast<const int*>(scratch + 4);
     const long long total = *reinterpret_cast<const long long*>(scratch + 8);
@@ -107,9 +108,11 @@ gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, 
     a.ticket = reinterpret_cast<unsigned int*>(s);
     a.error = reinterpret_cast<int*>(s + 4);
     a.total = reinterpret_cast<long long*>(s + 8);
+    a.nonempty = reinterpret_cast<unsigned int*>(s + 16);
     a.status = reinterpret_cast<unsigned long long*>(s + 64);
+    a.tile_list = reinterpret_cast<uint32_t*>(s + 64 + (size_t)a.ntiles * 8);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // the previous call's ticket, flags, count and look-back words must not leak into this one
+    // the previous call's ticket, flags, counts and tile words must not leak into this one
     e = cudaMemsetAsync(scratch, 0, 64 + (size_t)a.ntiles * 8, st);
     if (e == cudaSuccess && a.ntiles > 0) {
         if (gbt::volume_mode(v) == GBT_MODE_FIXED)

@@ -277,14 +277,13 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  * fails, or applications whose device memory is all owned by their own pool
  * or fixed budget.  gbt_extract_mesh may cudaMalloc scratch on a volume's
  * first mesh; this call never allocates: its scratch is one file-scope
- * device array of GBT_NOALLOC_SCRATCH_BYTES (1 MiB) that every GPU using the
+ * device array of GBT_NOALLOC_SCRATCH_BYTES (2 MiB) that every GPU using the
  * library holds until the process exits.  That limits it to volumes of at
  * most GBT_NOALLOC_MAX_CUBES cubes (a 512^3 grid fits); larger volumes get
  * GBT_ERR_INVALID_ARG.
  *
  * Output as gbt_extract_mesh_async: up to cap_tris triangles into verts/tris
- * and the count into the device word *d_n_tris (-1 if a bounded wait inside
- * the kernel gave up).  Asynchronous on `stream`.
+ * and the count into the device word *d_n_tris.  Asynchronous on `stream`.
  *
  * The first call on a device resolves the array's address (and may load the
  * library's device code), so make that first call before any stream capture.
@@ -292,8 +291,8 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  * each call clears it on `stream` first, and calls whose work overlaps on the
  * GPU (other streams, other host threads) race -- serialise them.
  * Failures are described by gbt_last_error(). */
-#define GBT_NOALLOC_SCRATCH_BYTES (1 << 20)
-#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64) / 8) * 1024)
+#define GBT_NOALLOC_SCRATCH_BYTES (2 << 20)
+#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64) / 12) * 1024)
 gbt_status gbt_extract_mesh_noalloc(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                     int64_t index_base, int64_t* d_n_tris, void* stream);
 
