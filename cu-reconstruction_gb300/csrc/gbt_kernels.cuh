@@ -705,70 +705,85 @@ __device__ __forceinline__ bool cube_xcorners(const McArgs& a, uint32_t c, uint3
 }
 
 // Types (0 for a cube that is not emitted: past the end, or in the fixed mode
-// with a corner of weight <= 0) of the lane's cubes cube[0..NB) -- each lane
-// of the warp holding the cube after the previous lane's -- with every load
-// of the NB cubes issued before any is used.  A cube past the end reads the
-// last cube, in bounds, and is discarded.
-template <int MODE, int NB>
-__device__ __forceinline__ void mc_types(const McArgs& a, const uint64_t (&cube)[NB], int lane, int (&type)[NB],
-                                         const unsigned char* s_type) {
-    float dx[NB][4], dn[NB][4];
-    float wx[NB][4], wn[NB][4];
-    bool own[NB];
+// with a corner of weight <= 0) of NG consecutive groups of 32 cubes from
+// cube `base` (a multiple of 32): lane l of group i holds cube
+// base + 32 i + l.  Every x-corner load of the NG groups is issued before any
+// is used.  The x + 1 corners of a cube are the next lane's x corners, or
+// for lane 31 the x corners of lane 0 of the next group; the last cube of a
+// grid row and lane 31 of the last group load theirs, under a branch the
+// warp takes only when one of its lanes needs it.  A cube past the end reads
+// the last cube, in bounds, and is discarded.
+template <int MODE, int NG>
+__device__ __forceinline__ void mc_warp_types(const McArgs& a, uint64_t base, int lane, int (&type)[NG],
+                                              const unsigned char* s_type) {
+    bool own[NG];
+    float dx[NG][4], wx[NG][4];
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-        const uint32_t c = cube[i] < a.ncubes ? (uint32_t)cube[i] : a.ncubes - 1;
+    for (int i = 0; i < NG; ++i) {
+        const uint64_t cube = base + 32 * i + lane;
+        const uint32_t c = cube < a.ncubes ? (uint32_t)cube : a.ncubes - 1;
         uint32_t idx[4];
-        own[i] = cube_xcorners<MODE>(a, c, idx) || lane == 31;
+        own[i] = cube_xcorners<MODE>(a, c, idx) || (i == NG - 1 && lane == 31);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             dx[i][k] = __ldg(a.D + idx[k]);
-            dn[i][k] = own[i] ? __ldg(a.D + idx[k] + 1) : 0.f;
-            if (MODE == kFixed) {
-                wx[i][k] = __ldg(a.W + idx[k]);
-                wn[i][k] = own[i] ? __ldg(a.W + idx[k] + 1) : 0.f;
+            if (MODE == kFixed) wx[i][k] = __ldg(a.W + idx[k]);
+        }
+    }
+    int so[NG];
+#pragma unroll
+    for (int i = 0; i < NG; ++i) {
+        so[i] = 0;
+        if (__any_sync(0xffffffffu, own[i]) && own[i]) {
+            // (the corner indices again, rather than kept live for the rare case)
+            const uint64_t cube = base + 32 * i + lane;
+            uint32_t idx[4];
+            cube_xcorners<MODE>(a, cube < a.ncubes ? (uint32_t)cube : a.ncubes - 1, idx);
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                so[i] |= (__ldg(a.D + idx[k] + 1) < 0.f) << k;
+                if (MODE == kFixed) ok = ok && __ldg(a.W + idx[k] + 1) > 0.f;
             }
+            if (MODE == kFixed) so[i] |= ok << 4;
+        }
+    }
+    int sx[NG];
+#pragma unroll
+    for (int i = 0; i < NG; ++i) {
+        sx[i] = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) sx[i] |= (dx[i][k] < 0.f) << k;
+        if (MODE == kFixed) {
+            const bool okx = wx[i][0] > 0.f && wx[i][1] > 0.f && wx[i][2] > 0.f && wx[i][3] > 0.f;
+            sx[i] |= okx << 4;
         }
     }
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-        int sx = 0, so = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            sx |= (dx[i][k] < 0.f) << k;
-            so |= (dn[i][k] < 0.f) << k;
-        }
-        if (MODE == kFixed) {
-            const bool okx = wx[i][0] > 0.f && wx[i][1] > 0.f && wx[i][2] > 0.f && wx[i][3] > 0.f;
-            const bool oko = wn[i][0] > 0.f && wn[i][1] > 0.f && wn[i][2] > 0.f && wn[i][3] > 0.f;
-            sx |= okx << 4;
-            so |= oko << 4;
-        }
-        // every lane takes part in the shuffle; a lane then keeps its own loads or the next lane's
-        const int nx = __shfl_down_sync(0xffffffffu, sx, 1);
-        const int sn = own[i] ? so : nx;
-        const int t = s_type[(sx & 15) | (sn & 15) << 4];
-        bool ok = cube[i] < a.ncubes;
-        if (MODE == kFixed) ok = ok && (sx & sn & 16);
+    for (int i = 0; i < NG; ++i) {
+        // every lane takes part in both shuffles
+        const int nx = __shfl_down_sync(0xffffffffu, sx[i], 1);
+        const int nf = __shfl_sync(0xffffffffu, sx[i + 1 < NG ? i + 1 : i], 0);
+        const int sn = own[i] ? so[i] : (lane == 31 ? nf : nx);
+        const int t = s_type[(sx[i] & 15) | (sn & 15) << 4];
+        bool ok = base + 32 * i + lane < a.ncubes;
+        if (MODE == kFixed) ok = ok && (sx[i] & sn & 16);
         type[i] = ok ? t : 0;
     }
 }
 
-// Types of the thread's cubes of a tile: cube c0 + i * kMcThreads + tid for
-// i < CPT, NB of them at a time (the fixed mode also loads weights: half as
-// many in flight).
+// Types of the thread's cubes of a tile: warp w holds the CPT consecutive
+// groups of 32 cubes from group w * CPT, classified NB groups at a time (the
+// fixed mode also loads weights: half as many in flight).
 template <int MODE, int CPT>
 __device__ __forceinline__ void mc_tile_types(const McArgs& a, uint32_t tile, int tid, int (&type)[CPT],
                                               const unsigned char* s_type) {
     constexpr int NB = MODE == kFixed ? 2 : 4;
-    const uint64_t c0 = (uint64_t)tile * (kMcThreads * CPT);
+    const uint64_t base = (uint64_t)tile * (kMcThreads * CPT) + (uint64_t)(tid >> 5) * (32 * CPT);
 #pragma unroll
     for (int i0 = 0; i0 < CPT; i0 += NB) {
-        uint64_t cube[NB];
         int t[NB];
-#pragma unroll
-        for (int i = 0; i < NB; ++i) cube[i] = c0 + (uint64_t)(i0 + i) * kMcThreads + tid;
-        mc_types<MODE, NB>(a, cube, tid & 31, t, s_type);
+        mc_warp_types<MODE, NB>(a, base + 32 * i0, tid & 31, t, s_type);
 #pragma unroll
         for (int i = 0; i < NB; ++i) type[i0 + i] = t[i];
     }
@@ -785,38 +800,127 @@ __device__ __forceinline__ void mc_load_tables(unsigned char* s_count, unsigned 
 }
 
 // Marching cubes in three launches, none of which waits on another CTA.
-// (1) mc_count_kernel: warps classify groups of 32 consecutive cubes and add
-//     each group's triangle count to its tile's word (tiles of
-//     mc_tile_cubes(MODE) cubes in linear cube order; the words start at 0).
+// (1) mc_count_kernel: a warp takes a segment of kMcSegCubes cubes along x in
+//     one cube layer and walks kMcRowsPerTask rows along y.  Lane l holds
+//     voxel column x0 + l; per row it loads its voxels at (y+1, z) and
+//     (y+1, z+1) -- two distance loads per cube (four in the fixed mode) --
+//     and the previous row's two sign bits complete the nibble of its cube's
+//     x corners; the x + 1 nibble is the next lane's.  Each row's triangle
+//     counts go to the words of the tiles (mc_tile_cubes(MODE) cubes in
+//     linear cube order, words starting at 0) its cubes fall in.
 // (2) mc_scan_kernel: one CTA turns the tile counts into exclusive offsets in
 //     place, lists the tiles that have triangles, and writes the total.
 // (3) mc_emit_kernel: CTAs take listed tiles by ticket, classify the tile
 //     again, scan its counts and write its triangles from the tile's offset.
 // Triangles come out in the reference's linear cube order.
+constexpr uint32_t kMcSegCubes = 31;      // cubes per segment: 32 voxel columns
+constexpr uint32_t kMcRowsPerTask = 64;   // rows a warp walks per task
+constexpr uint32_t kMcRowBatch = 8;       // rows whose loads are in flight together
+constexpr int kMcTileShift[2] = {11, 10};  // log2 of mc_tile_cubes(mode)
+
 template <int MODE>
 __global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_constant__ McArgs a) {
-    __shared__ unsigned char s_count[256];
-    __shared__ unsigned char s_type[256];
-    mc_load_tables(s_count, nullptr, nullptr, s_type);
+    // triangles of the cube whose x-corner nibble is q & 15 and x + 1 nibble q >> 4
+    __shared__ unsigned char s_cnt[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) s_cnt[k] = GBT_MC_TRI_COUNT[mc_type_of_nibbles(k & 15, k >> 4)];
     __syncthreads();
-    constexpr uint64_t kTile = mc_tile_cubes(MODE);
-    constexpr int NB = MODE == kFixed ? 2 : 4;
+    static_assert((1 << kMcTileShift[MODE]) == mc_tile_cubes(MODE), "tiles of a power of two cubes");
+    static_assert(mc_tile_cubes(MODE) >= 2 * 32, "a row segment straddles at most one tile boundary");
+    constexpr int kShift = kMcTileShift[MODE];
     const int lane = threadIdx.x & 31;
+    const uint32_t gx = (uint32_t)a.gx, gy = (uint32_t)a.gy;
+    const uint32_t cx_n = gx - 1, cy_n = gy - 1, cz_n = (uint32_t)a.gz - 1;
+    const uint32_t nseg = (cx_n + kMcSegCubes - 1) / kMcSegCubes;
+    const uint32_t nchunk = (cy_n + kMcRowsPerTask - 1) / kMcRowsPerTask;
+    const uint64_t ntasks = (uint64_t)cz_n * nchunk * nseg;
+    const uint32_t layer = (MODE == kCompat) ? gx + gy : gx * gy;   // marching_cubes.cu:211
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint64_t ngroups = ((uint64_t)a.ncubes + 31) / 32;
     // the loop bound is the same for all lanes of a warp
-    for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += NB * nwarps) {
-        uint64_t cube[NB];
-        int t[NB];
+    for (uint64_t task = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntasks; task += nwarps) {
+        const uint32_t seg = (uint32_t)(task % nseg);
+        const uint64_t rest = task / nseg;
+        const uint32_t chunk = (uint32_t)(rest % nchunk);
+        const uint32_t cz = (uint32_t)(rest / nchunk);
+        const uint32_t x0 = seg * kMcSegCubes;
+        const uint32_t x = x0 + (uint32_t)lane;                            // this lane's voxel column
+        const bool cube_ok = lane < (int)kMcSegCubes && x < cx_n;          // ... and its cube
+        const uint32_t xl = x < gx ? x : gx - 1;                           // loads stay in the grid
+        const uint32_t y0 = chunk * kMcRowsPerTask;
+        const uint32_t y1 = min(y0 + kMcRowsPerTask, cy_n);
+        const uint32_t i0 = cz * layer + y0 * gx + xl;                     // voxel (x, y0, z); +layer: z+1
+        const float* d0p = a.D + i0;
+        const float* d1p = d0p + layer;
+        const float* w0p = a.W + i0;
+        const float* w1p = w0p + layer;
+        int lo = (__ldg(d0p) < 0.f) | (__ldg(d1p) < 0.f) << 1;            // row y: corners 0, 3
+        bool lo_ok = true;
+        if (MODE == kFixed) lo_ok = __ldg(w0p) > 0.f && __ldg(w1p) > 0.f;
+        // linear cube index (below 2^32: the grid has fewer voxels); the
+        // warp's cubes of a row lie in tile `cur` or cur + 1, cur being lane 0's
+        uint32_t c = (cz * cy_n + y0) * cx_n + x;
+        uint32_t c_lane0 = c - (uint32_t)lane;
+        uint32_t cur = c_lane0 >> kShift;
+        unsigned acc0 = 0, acc1 = 0;   // this lane's triangles in tiles cur and cur + 1
+        auto flush = [&]() {
+            const unsigned n0 = __reduce_add_sync(0xffffffffu, acc0);
+            const unsigned n1 = __reduce_add_sync(0xffffffffu, acc1);
+            if (lane == 0) {
+                if (n0) atomicAdd(a.status + cur, (unsigned long long)n0);
+                if (n1) atomicAdd(a.status + cur + 1, (unsigned long long)n1);
+            }
+            acc0 = 0;
+            acc1 = 0;
+        };
+        auto row = [&](float d0, float d1, float w0, float w1) {
+            if ((c_lane0 >> kShift) != cur) {   // the same for the whole warp
+                flush();
+                cur = c_lane0 >> kShift;
+            }
+            const int hi = (d0 < 0.f) | (d1 < 0.f) << 1;   // row y+1: corners 4, 7
+            bool hi_ok = true;
+            if (MODE == kFixed) hi_ok = w0 > 0.f && w1 > 0.f;
+            int sx = lo | hi << 2;
+            if (MODE == kFixed) sx |= (lo_ok && hi_ok) << 4;
+            const int sn = __shfl_down_sync(0xffffffffu, sx, 1);
+            unsigned n = s_cnt[(sx & 15) | (sn & 15) << 4];
+            if (!cube_ok || (MODE == kFixed && !(sx & sn & 16))) n = 0u;
+            if ((c >> kShift) == cur) acc0 += n; else acc1 += n;
+            lo = hi;
+            lo_ok = hi_ok;
+            c += cx_n;
+            c_lane0 += cx_n;
+        };
+        // full batches of kMcRowBatch rows: every load of a batch is issued
+        // before any is used (the tile-word atomics would otherwise keep the
+        // compiler from moving the next row's loads ahead)
+        uint32_t y = y0;
+        for (; y + kMcRowBatch <= y1; y += kMcRowBatch) {
+            float d0[kMcRowBatch], d1[kMcRowBatch], w0[kMcRowBatch], w1[kMcRowBatch];
 #pragma unroll
-        for (int i = 0; i < NB; ++i) cube[i] = (g + i * nwarps) * 32 + lane;
-        mc_types<MODE, NB>(a, cube, lane, t, s_type);
+            for (uint32_t j = 0; j < kMcRowBatch; ++j) {
+                const size_t off = (size_t)(j + 1) * gx;
+                d0[j] = __ldg(d0p + off);
+                d1[j] = __ldg(d1p + off);
+                if (MODE == kFixed) {
+                    w0[j] = __ldg(w0p + off);
+                    w1[j] = __ldg(w1p + off);
+                }
+            }
 #pragma unroll
-        for (int i = 0; i < NB; ++i) {
-            const unsigned n = __reduce_add_sync(0xffffffffu, (unsigned)s_count[t[i]]);
-            const uint64_t gi = g + i * nwarps;
-            if (lane == 0 && n != 0u && gi < ngroups) atomicAdd(a.status + gi * 32 / kTile, (unsigned long long)n);
+            for (uint32_t j = 0; j < kMcRowBatch; ++j) row(d0[j], d1[j], MODE == kFixed ? w0[j] : 0.f, MODE == kFixed ? w1[j] : 0.f);
+            d0p += (size_t)kMcRowBatch * gx;
+            d1p += (size_t)kMcRowBatch * gx;
+            w0p += (size_t)kMcRowBatch * gx;
+            w1p += (size_t)kMcRowBatch * gx;
         }
+        for (; y < y1; ++y) {   // the rows after the last full batch
+            d0p += gx;
+            d1p += gx;
+            w0p += gx;
+            w1p += gx;
+            row(__ldg(d0p), __ldg(d1p), MODE == kFixed ? __ldg(w0p) : 0.f, MODE == kFixed ? __ldg(w1p) : 0.f);
+        }
+        flush();
     }
 }
 
@@ -833,11 +937,15 @@ __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_co
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t per = (n + kMcScanThreads - 1) / kMcScanThreads;
     const uint32_t b = min(tid * per, n), e = min(b + per, n);
+    // the thread's words are read 8 at a time, all 8 loads in flight together
+    constexpr uint32_t kBatch = 8;
     unsigned long long own = 0;
-#pragma unroll 8
-    for (uint32_t i = b; i < e; ++i) {
-        const unsigned long long c = a.status[i];
-        own += (c << 24) | (c != 0ull ? 1ull : 0ull);
+    for (uint32_t i = b; i < e; i += kBatch) {
+        unsigned long long c[kBatch];
+#pragma unroll
+        for (uint32_t j = 0; j < kBatch; ++j) c[j] = i + j < e ? a.status[i + j] : 0ull;
+#pragma unroll
+        for (uint32_t j = 0; j < kBatch; ++j) own += (c[j] << 24) | (c[j] != 0ull ? 1ull : 0ull);
     }
     unsigned long long x = own;
 #pragma unroll
@@ -861,11 +969,17 @@ __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_co
     const unsigned long long excl = s_part[warp] + x - own;
     unsigned long long off = excl >> 24;
     uint32_t k = (uint32_t)(excl & 0xffffffull);
-    for (uint32_t i = b; i < e; ++i) {
-        const unsigned long long c = a.status[i];
-        a.status[i] = off;
-        if (c) a.tile_list[k++] = i;
-        off += c;
+    for (uint32_t i = b; i < e; i += kBatch) {
+        unsigned long long c[kBatch];
+#pragma unroll
+        for (uint32_t j = 0; j < kBatch; ++j) c[j] = i + j < e ? a.status[i + j] : 0ull;
+#pragma unroll
+        for (uint32_t j = 0; j < kBatch; ++j) {
+            if (i + j >= e) break;
+            a.status[i + j] = off;
+            if (c[j]) a.tile_list[k++] = i + j;
+            off += c[j];
+        }
     }
     if (tid == kMcScanThreads - 1) {
         const unsigned long long all = excl + own;
@@ -920,7 +1034,7 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
                 if (lane >= o) n += y;
             }
             incl[i] = n;
-            if (lane == 31) s_wsum[i * kWarps + warp] = n;
+            if (lane == 31) s_wsum[warp * CPT + i] = n;   // group warp * CPT + i of the tile
         }
         __syncthreads();
         if (warp == 0) {
@@ -952,9 +1066,9 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
             const int t = type[i];
             const int n = s_count[t];
             if (!n) continue;
-            long long out = tile_prefix + s_wsum[i * kWarps + warp] + incl[i] - n;
+            long long out = tile_prefix + s_wsum[warp * CPT + i] + incl[i] - n;
             if (out >= a.cap) continue;
-            const uint32_t c = c0 + i * kMcThreads + tid;
+            const uint32_t c = c0 + (warp * CPT + i) * 32 + lane;
             const uint32_t row = fastdiv(c, a.div_cx);
             const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
             const uint32_t cz = fastdiv(row, a.div_cy);
@@ -1310,9 +1424,12 @@ cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
         if (per_count < 1) per_count = 1;
         if (per_emit < 1) per_emit = 1;
     }
-    const long long groups_per_cta = kMcThreads / 32 * (MODE == kFixed ? 2 : 4);
+    // one warp per task (a segment of a cube layer, kMcRowsPerTask rows)
+    const long long nseg = (a.gx - 1 + (long long)kMcSegCubes - 1) / kMcSegCubes;
+    const long long nchunk = (a.gy - 1 + (long long)kMcRowsPerTask - 1) / kMcRowsPerTask;
+    const long long ntasks = (long long)(a.gz - 1) * nchunk * nseg;
     long long grid = (long long)sms * per_count;
-    const long long need = ((long long)a.ncubes + 32 * groups_per_cta - 1) / (32 * groups_per_cta);
+    const long long need = (ntasks + kMcThreads / 32 - 1) / (kMcThreads / 32);
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
     mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);

@@ -23,7 +23,9 @@ def smooth_field(shape, seed, scale=0.05):
     return (scale * f / 5).astype(np.float32)
 
 
-@pytest.mark.parametrize("grid", [(64, 48, 40), (77, 50, 37), (2, 2, 2), (130, 3, 9)])
+# (64, 130, 5): 63 cubes per row (two segments of 31 and one of 1), 129 rows
+# per layer (two runs of 64 rows and one of 1)
+@pytest.mark.parametrize("grid", [(64, 48, 40), (77, 50, 37), (2, 2, 2), (130, 3, 9), (64, 130, 5)])
 def test_compat_ieee_mesh_bitexact(gpu, oracle, grid):
     tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=tuple(0.01 * g for g in grid),
                           global_offset=(-0.3, 0.2, 0.5), arith="ieee")
@@ -37,7 +39,7 @@ def test_compat_ieee_mesh_bitexact(gpu, oracle, grid):
     assert np.array_equal(V.view(np.uint32), Vo.view(np.uint32))
 
 
-@pytest.mark.parametrize("grid", [(64, 48, 40), (77, 50, 37), (33, 65, 17)])
+@pytest.mark.parametrize("grid", [(64, 48, 40), (77, 50, 37), (33, 65, 17), (129, 66, 6)])
 def test_fixed_mesh_bitexact(gpu, oracle, grid):
     tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=tuple(0.01 * g for g in grid),
                           global_offset=(-0.3, 0.2, 0.5), mode="fixed", max_weight=16)
