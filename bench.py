@@ -715,7 +715,7 @@ def multiscene(args, torch, rank, world, local):
     else:
         mine = list(range(16))
     cam = S.Camera()
-    vols, depths, poses, sizes, nfs = [], [], [], [], []
+    vols, depths, poses, sizes, nfs, frames3d = [], [], [], [], [], []
     for i in mine:
         n, nf = specs[i]
         sid = i if split else shard.scene_seed(0, rank, i)
@@ -725,6 +725,7 @@ def multiscene(args, torch, rank, world, local):
         tc = TSDFVolumeConfig(**S.grid_for(n, 2.56), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy,
                               max_weight=128.0, mode=args.mode)
         vols.append(TSDFVolume(tc))
+        frames3d.append(fr)
         depths.append([fr[k] for k in range(nf)])
         poses.append(ps)
         sizes.append(n)
@@ -816,23 +817,31 @@ def multiscene(args, torch, rank, world, local):
         e1.record(stream)
         e1.synchronize()
         per_scene.append({"grid": n, "frames": f, "voxel_updates_per_s": n ** 3 * f / (e0.elapsed_time(e1) * 1e-3)})
-    # end to end: depth frames from pinned host memory, integrate, meshes back to the host
-    host = [[torch.empty(d.shape, dtype=d.dtype, pin_memory=True).copy_(d) for d in ds] for ds in depths]
+    # end to end through the public API: depth frames from pinned host memory
+    # (copied window by window while the previous window integrates), the
+    # meshes of all scenes, their counts and triangles back to the host
+    host = [torch.empty(f.shape, dtype=f.dtype, pin_memory=True).copy_(f) for f in frames3d]
+    counts = torch.zeros(len(vols), dtype=torch.int64, device="cuda")
     torch.cuda.synchronize()
     e2e = []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for hs, ds in zip(host, depths):
-            for h, d in zip(hs, ds):
-                d.copy_(h, non_blocking=True)
-        step_integrate()
-        meshes = [extract_mesh_device(v, capacity=c) for v, c in zip(vols, caps)]
-        d2h = sum(m[0].cpu().numel() * 4 + m[1].cpu().numel() * 4 + 8 for m in meshes)
+        for v in vols:
+            v.reset()
+        batch.integrate_streamed(vols, host, frames3d, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)
+        sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for k, (v, (vb, tb, _), cap) in enumerate(zip(vols, outs, caps)):
+            L.check(lib.gbt_extract_mesh_async(v.handle, C.c_void_p(vb.data_ptr()), C.c_void_p(tb.data_ptr()), cap,
+                                               0, C.c_void_p(counts[k:k + 1].data_ptr()), sh))
+        ns = counts.cpu().tolist()
+        d2h = 8 * len(ns)
+        for n, (vb, tb, _) in zip(ns, outs):
+            d2h += vb[:n].cpu().numel() * 4 + tb[:n].cpu().numel() * 4
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e.append(time.perf_counter() - t0)
-    h2d = sum(d.numel() * d.element_size() for ds in depths for d in ds)
+    h2d = sum(h.numel() * h.element_size() for h in host)
     value = job_updates * args.steps / (total_ms * 1e-3)
     e2e_value = shard.whole_job_rate(updates, float(np.mean(e2e)))
     if rank != 0:
@@ -1068,16 +1077,23 @@ def main():
     peak, peak_kind = peaks()
 
     # end to end through the public API with host buffers: H2D of the step's
-    # depth frames from pinned memory, integrate, mesh, D2H of the mesh
+    # depth frames from pinned memory (on the batched path window by window,
+    # overlapped with the previous window's launch), integrate, mesh, D2H of
+    # the mesh
     e2e_ms = []
     h2d = frames_host.numel() * 2
     d2h = 0
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        frames_dev.copy_(frames_host, non_blocking=True)
         vol.reset()
-        integrate_all()
+        if path == "batched":
+            # window w + 1 copies while window w integrates
+            batch.integrate_streamed([vol], [frames_host], [frames_dev], [poses], brick=brick, ctas_per_sm=ctas,
+                                     frames_per_launch=K)
+        else:
+            frames_dev.copy_(frames_host, non_blocking=True)
+            integrate_all()
         V, T = extract_mesh_device(vol, capacity=cap)
         Vh = V.cpu()
         Th = T.cpu()

@@ -88,3 +88,32 @@ def test_batch_rejects_mixed_modes(gpu):
     bi = BatchIntegrator(4, 8)
     with pytest.raises(L.GbtError, match="same mode"):
         bi.integrate([a, b], [[d], [d]], [[np.array([1.0, 0, 0, 0, 0, 0, 0])]] * 2)
+
+
+@pytest.mark.parametrize("mode,fmt", [("compat", "u16"), ("fixed", "u16"), ("compat", "f32")])
+def test_streamed_from_host_equals_device_integrate(gpu, mode, fmt):
+    """integrate_streamed copies window w + 1 from pinned host memory while
+    window w integrates; the volumes equal a plain batched call on frames
+    already on the device."""
+    cfgs, vols, depths, poses = scene_data(gpu, mode)
+    cam = S.Camera.half()
+    host, dev = [], []
+    for i, (grid, nf) in enumerate(SCENES):
+        seq = S.make_sequence(nf, scene_id=10 + i, camera=cam, trajectory="circle")
+        d = np.ascontiguousarray(seq.depth_u16 if fmt == "u16" else seq.depth_m())
+        host.append(gpu.from_numpy(d.view(np.int16) if fmt == "u16" else d).pin_memory())
+        dev.append(gpu.empty(host[-1].shape, dtype=host[-1].dtype, device="cuda"))
+        depths[i] = [dev_depth(gpu, x) for x in d]
+    b = BatchIntegrator(max_scenes=8, max_frames=512)
+    b.integrate(vols, depths, poses, frames_per_launch=16)
+    gpu.cuda.synchronize()
+    expect = [(v.voxel_weights_data().cpu().numpy(), v.voxel_distances_data().cpu().numpy()) for v in vols]
+    for v in vols:
+        v.reset()
+    b.integrate_streamed(vols, host, dev, poses, frames_per_launch=16)
+    gpu.cuda.synchronize()
+    for (W0, D0), v, h, d in zip(expect, vols, host, dev):
+        assert np.array_equal(d.cpu().numpy(), h.numpy())
+        assert np.array_equal(v.voxel_weights_data().cpu().numpy(), W0)
+        assert np.array_equal(v.voxel_distances_data().cpu().numpy().view(np.uint32), D0.view(np.uint32))
+    assert (expect[2][0] > 0).mean() > 0.05
