@@ -644,6 +644,9 @@ gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_
         a.frames = reinterpret_cast<const gbt::FrameDesc*>(a.scenes + b->max_scenes);
         a.w0 = w * frames_per_launch;
         a.wn = frames_per_launch;
+        a.rows_of_4 = 1;
+        for (int j = 0; j < nitems; ++j)
+            if (items[j].volume->desc.nx % 4 != 0) a.rows_of_4 = 0;
         int m = 0;
         while (m < nitems && hs[m].nframes > a.w0) ++m;
         a.nscenes = m;

@@ -77,7 +77,7 @@ struct BatchArgs {
     const FrameDesc* frames;
     int32_t nscenes;        // scenes with frames in this window
     int32_t w0, wn;         // frame window
-    int32_t pad0;
+    int32_t rows_of_4;      // 1: every scene's x extent is a multiple of 4
     long long total_bricks; // bricks of those scenes
     unsigned int* ticket;   // this launch's ticket, zero at launch
 };

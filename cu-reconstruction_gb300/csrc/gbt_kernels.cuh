@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
 // scenes by frames per voxel, most expensive first); CTAs take the next brick
 // from an atomic ticket, so uneven scenes balance dynamically.  A brick of a
 // scene receives all of that scene's frames, in order, in registers.
-template <int MODE, int TX, int BY, int BZ>
+template <int MODE, int TX, int BY, int BZ, bool FULL>
 __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_constant__ BatchArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
     __shared__ FrameSlot s_frame[kBatchMaxFrames];
@@ -628,13 +628,13 @@ __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_const
         ThreadVoxels t;
         if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
         t.load(v);
-        // (a copy specialised for rows of 4 voxels, as the pass kernel has,
-        // needs 72 registers here against 64 and is slower)
+        // FULL: every scene's x extent is a multiple of 4, so every thread
+        // has 4 voxels (the host picks the instance)
         bool dirty = false;
 #pragma unroll
         for (int c = 0; c < kBatchMaxFrames / 32; ++c)
-            dirty |= apply_frames<MODE, false>(v, s_frame + c * 32, masks[c], t.px, t.py, t.pz, t.nvalid, t.d, t.w,
-                                               s_inv);
+            dirty |= apply_frames<MODE, FULL>(v, s_frame + c * 32, masks[c], t.px, t.py, t.pz, t.nvalid, t.d, t.w,
+                                              s_inv);
         if (dirty) t.store(v);
     }
 }
@@ -1371,7 +1371,10 @@ cudaError_t launch_integrate_mode(const IntegrateArgs& a, int brick, int grid, c
 
 template <int MODE, int TX, int BY, int BZ>
 cudaError_t launch_batch_shape(const BatchArgs& a, int grid, cudaStream_t s) {
-    integrate_batch_kernel<MODE, TX, BY, BZ><<<grid, 128, 0, s>>>(a);
+    if (a.rows_of_4)
+        integrate_batch_kernel<MODE, TX, BY, BZ, true><<<grid, 128, 0, s>>>(a);
+    else
+        integrate_batch_kernel<MODE, TX, BY, BZ, false><<<grid, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1396,7 +1399,7 @@ int resident_128(Kernel k) {
 
 template <int MODE, int TX, int BY, int BZ>
 int resident_shape(bool batched) {
-    return batched ? resident_128(integrate_batch_kernel<MODE, TX, BY, BZ>)
+    return batched ? resident_128(integrate_batch_kernel<MODE, TX, BY, BZ, true>)
                    : resident_128(integrate_kernel<MODE, TX, BY, BZ>);
 }
 
