@@ -862,7 +862,8 @@ def multiscene(args, torch, rank, world, local):
         "per_scene": per_scene,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e))},
-        "gpu_launches": args.steps * (2 * len(vols) + ((max(nfs) + fpl - 1) // fpl)),
+        # per step: a reset per volume, the batched launches, three mesh launches per volume
+        "gpu_launches": args.steps * (4 * len(vols) + ((max(nfs) + fpl - 1) // fpl)),
         "clocks": clocks.summary(),
         "autotune": {"candidates": len(table)},
     }
@@ -1075,6 +1076,24 @@ def main():
     # pass kernel and the fixed mode: not captured.
     traffic = (12.31 * nvox + (nf / n_passes) * frame_px * 2) if (path == "batched" and args.mode == "compat") else None
     peak, peak_kind = peaks()
+    # The kernel is bound by instruction issue, not by HBM (a window of K
+    # frames shares each voxel's 16 bytes).  Its issue roofline: warp
+    # instructions per voxel-update from one ncu capture of this kernel (320^3,
+    # 64-frame window: 1.675 G warp instructions for 2.097 G updates), times
+    # the measured update rate, against one instruction per clock on each of
+    # the 4 schedulers of every SM at the median SM clock sampled while timing.
+    issue = None
+    if path == "batched" and args.mode == "compat":
+        warp_inst_per_update = 1.675292e9 / (320 ** 3 * 64)
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+        sm_mhz = (clocks.summary().get("sm_mhz") or 0.0)
+        upd_per_s = nvox * (nf / n_passes) / (launch_ms * 1e-3)
+        if sm_mhz > 0:
+            achieved_i = warp_inst_per_update * upd_per_s
+            peak_i = 4.0 * sm_count * sm_mhz * 1e6
+            issue = {"unit": "warp instructions/s", "achieved": achieved_i, "peak": peak_i, "frac": achieved_i / peak_i,
+                     "warp_instructions_per_update": warp_inst_per_update, "sm_mhz": sm_mhz, "sms": sm_count,
+                     "source": "instructions per update: ncu capture of integrate_batch_kernel at 320^3, 64 frames"}
 
     # end to end through the public API with host buffers: H2D of the step's
     # depth frames from pinned memory (on the batched path window by window,
@@ -1129,14 +1148,16 @@ def main():
                      "traffic": traffic,
                      "kernel": "integrate_batch_kernel" if path == "batched" else "integrate_kernel",
                      "launch_ms": launch_ms,
-                     "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind},
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind,
+                     "issue": issue},
         "breakdown_ms": {"reset": float(np.mean([ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)])),
                          "integrate": float(np.mean(int_ms)), "mesh": float(np.mean(mesh_ms))},
         "integrate_only": {"value": nvox * nf / (float(np.mean(int_ms)) * 1e-3), "unit": UNIT},
         "mesh": {"triangles_per_s": ntri / (float(np.mean(mesh_ms)) * 1e-3) if ntri else 0.0, "triangles": ntri},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": float(np.mean(e2e_ms))},
-        "gpu_launches": args.steps * (1 + n_passes + 1),
+        # per step: reset, the integrate launches, three mesh launches (count, scan, emit)
+        "gpu_launches": args.steps * (1 + n_passes + 3),
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
         "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": candidates},

@@ -14,10 +14,10 @@ pytestmark = pytest.mark.gpu
 SCENES = [((64, 64, 64), 10), ((40, 56, 72), 37), ((96, 80, 48), 140), ((20, 20, 20), 1), ((33, 17, 9), 5)]
 
 
-def scene_data(gpu, mode, arith="reference"):
+def scene_data(gpu, mode, arith="reference", scenes=SCENES):
     cam = S.Camera.half()
     vols, depths, poses, cfgs = [], [], [], []
-    for i, (grid, nf) in enumerate(SCENES):
+    for i, (grid, nf) in enumerate(scenes):
         seq = S.make_sequence(nf, scene_id=10 + i, camera=cam, trajectory="circle")
         tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=tuple(2.56 * g / max(grid) for g in grid),
                               global_offset=(-1.28, -1.0, -1.28), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx,
@@ -45,6 +45,24 @@ def test_batch_equals_per_volume_integrate(gpu, mode, arith, brick):
         assert np.array_equal(W0, W1)
         assert np.array_equal(D0.view(np.uint32), D1.view(np.uint32))
     assert (vols[2].voxel_weights_data() > 0).float().mean().item() > 0.05
+
+
+@pytest.mark.parametrize("mode,arith", [("fixed", "ieee"), ("compat", "reference")])
+def test_batch_of_rows_of_4_equals_per_volume_integrate(gpu, mode, arith):
+    """Every scene's x extent a multiple of 4: the batched kernel's instance
+    without per-voxel count checks."""
+    scenes = [s for s in SCENES if s[0][0] % 4 == 0]
+    assert len(scenes) == 4
+    cfgs, vols, depths, poses = scene_data(gpu, mode, arith, scenes)
+    BatchIntegrator(max_scenes=8, max_frames=512).integrate(vols, depths, poses, brick=2, frames_per_launch=64)
+    gpu.cuda.synchronize()
+    for tc, vol, ds, ps in zip(cfgs, vols, depths, poses):
+        ref = TSDFVolume(tc)
+        ref.integrate_sequence(ds, ps, frames_per_pass=32)
+        gpu.cuda.synchronize()
+        assert np.array_equal(ref.voxel_weights_data().cpu().numpy(), vol.voxel_weights_data().cpu().numpy())
+        assert np.array_equal(ref.voxel_distances_data().cpu().numpy().view(np.uint32),
+                              vol.voxel_distances_data().cpu().numpy().view(np.uint32))
 
 
 def test_batch_chunks_and_graph_replay(gpu):
