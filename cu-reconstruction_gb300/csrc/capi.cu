@@ -334,8 +334,11 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     }
     int bx, by, bz;
     gbt::brick_extent(brick, &bx, &by, &bz);
-    const long long nbricks = (long long)((v->desc.nx + bx - 1) / bx) * ((v->desc.ny + by - 1) / by) *
-                              ((v->desc.nz + bz - 1) / bz);
+    const uint32_t nbx = (uint32_t)((v->desc.nx + bx - 1) / bx), nby = (uint32_t)((v->desc.ny + by - 1) / by);
+    const long long nbricks = (long long)nbx * nby * ((v->desc.nz + bz - 1) / bz);   // below 2^32: fewer than voxels
+    a.nbricks = (uint32_t)nbricks;
+    a.div_nbx = gbt::make_fastdiv(nbx);
+    a.div_nby = gbt::make_fastdiv(nby);
     long long grid = (long long)device_sms() *
                      (ctas_per_sm ? ctas_per_sm
                                   : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith, false, brick));
@@ -617,6 +620,8 @@ gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_
         sc.nbx = (sc.vol.nx + bx - 1) / bx;
         sc.nby = (sc.vol.ny + by - 1) / by;
         sc.nbz = (sc.vol.nz + bz - 1) / bz;
+        sc.div_nbx = gbt::make_fastdiv((uint32_t)sc.nbx);
+        sc.div_nby = gbt::make_fastdiv((uint32_t)sc.nby);
         sc.brick_begin = bricks;
         bricks += (long long)sc.nbx * sc.nby * sc.nbz;
         if (it.volume->cfg.mode == GBT_MODE_FIXED)

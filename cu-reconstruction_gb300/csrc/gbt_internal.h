@@ -49,39 +49,6 @@ struct __align__(16) FrameSlot {
 };
 static_assert(sizeof(FrameSlot) == 80, "five 16-byte words");
 
-struct IntegrateArgs {
-    VolDesc vol;
-    int32_t nframes;
-    int32_t pad0;
-    FrameDesc frames[GBT_MAX_FRAMES_PER_PASS];
-};
-
-// Many volumes in one launch.  A scene's bricks are numbered from
-// brick_begin; frames [first_frame, first_frame + nframes) of the frame table
-// go into its volume.  One launch applies the window [w0, w0 + wn) of every
-// scene's frames (wn <= kBatchMaxFrames); scenes are sorted by frame count,
-// so the scenes with frames in a window are a prefix of the table.
-constexpr int kBatchMaxFrames = GBT_MAX_FRAMES_PER_SCENE_PASS;
-
-struct BatchScene {
-    VolDesc vol;
-    int32_t first_frame;
-    int32_t nframes;
-    int32_t nbx, nby, nbz;
-    int32_t pad0;
-    long long brick_begin;
-};
-
-struct BatchArgs {
-    const BatchScene* scenes;
-    const FrameDesc* frames;
-    int32_t nscenes;        // scenes with frames in this window
-    int32_t w0, wn;         // frame window
-    int32_t rows_of_4;      // 1: every scene's x extent is a multiple of 4
-    long long total_bricks; // bricks of those scenes
-    unsigned int* ticket;   // this launch's ticket, zero at launch
-};
-
 // Unsigned 32-bit division by a run-time invariant divisor with one
 // multiply-high, after Granlund & Montgomery, "Division by invariant integers
 // using multiplication" (PLDI 1994), figure 4.1.
@@ -101,6 +68,43 @@ inline FastDiv make_fastdiv(uint32_t d) {
     f.s = l;
     return f;
 }
+
+struct IntegrateArgs {
+    VolDesc vol;
+    int32_t nframes;
+    uint32_t nbricks;        // bricks of the volume for the launch's brick shape
+    FastDiv div_nbx;         // bricks along x
+    FastDiv div_nby;         // bricks along y
+    FrameDesc frames[GBT_MAX_FRAMES_PER_PASS];
+};
+
+// Many volumes in one launch.  A scene's bricks are numbered from
+// brick_begin; frames [first_frame, first_frame + nframes) of the frame table
+// go into its volume.  One launch applies the window [w0, w0 + wn) of every
+// scene's frames (wn <= kBatchMaxFrames); scenes are sorted by frame count,
+// so the scenes with frames in a window are a prefix of the table.
+constexpr int kBatchMaxFrames = GBT_MAX_FRAMES_PER_SCENE_PASS;
+
+struct BatchScene {
+    VolDesc vol;
+    int32_t first_frame;
+    int32_t nframes;
+    int32_t nbx, nby, nbz;
+    int32_t pad0;
+    FastDiv div_nbx;         // nbx
+    FastDiv div_nby;         // nby
+    long long brick_begin;
+};
+
+struct BatchArgs {
+    const BatchScene* scenes;
+    const FrameDesc* frames;
+    int32_t nscenes;        // scenes with frames in this window
+    int32_t w0, wn;         // frame window
+    int32_t rows_of_4;      // 1: every scene's x extent is a multiple of 4
+    long long total_bricks; // bricks of those scenes
+    unsigned int* ticket;   // this launch's ticket, zero at launch
+};
 
 // Marching cubes over the linear cube order (z, y, x) in tiles of
 // mc_tile_cubes(mode) cubes: counted per tile, offsets by a scan of the tile

@@ -549,13 +549,14 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
 
     const BrickLayout<TX, BY, BZ> L(tid);
     const int BXV = 4 * TX;
-    const int nbx = (v.nx + BXV - 1) / BXV, nby = (v.ny + BY - 1) / BY, nbz = (v.nz + BZ - 1) / BZ;
-    const long long nbricks = (long long)nbx * nby * nbz;
+    // brick numbers are below 2^32 (the volume has fewer voxels): 32-bit
+    // division by the host's invariant divisors
+    const uint32_t nbx = a.div_nbx.d, nby = a.div_nby.d;
 
-    for (long long b = blockIdx.x; b < nbricks; b += gridDim.x) {
-        const int bxi = (int)(b % nbx);
-        const long long rest = b / nbx;
-        const int bx0 = bxi * BXV, by0 = (int)(rest % nby) * BY, bz0 = (int)(rest / nby) * BZ;
+    for (uint32_t b = blockIdx.x; b < a.nbricks; b += gridDim.x) {
+        const uint32_t rest = fastdiv(b, a.div_nbx);
+        const uint32_t bzi = fastdiv(rest, a.div_nby);
+        const int bx0 = (int)(b - rest * nbx) * BXV, by0 = (int)(rest - bzi * nby) * BY, bz0 = (int)bzi * BZ;
         // frames for which this warp's box may contain an updated voxel
         const uint32_t fmask = warp_live_frames<MODE>(v, s_frame, 0, nf, L, bx0, by0, bz0);
         if (fmask == 0u) continue;
@@ -612,10 +613,11 @@ __global__ void __launch_bounds__(128) integrate_batch_kernel(const __grid_const
             for (int f = tid; f < nf; f += blockDim.x) load_slot<MODE>(frames[f], s_frame[f]);
             __syncthreads();
         }
-        const long long b = task - S.brick_begin;
-        const int bxi = (int)(b % S.nbx);
-        const long long rest = b / S.nbx;
-        const int bx0 = bxi * BXV, by0 = (int)(rest % S.nby) * BY, bz0 = (int)(rest / S.nby) * BZ;
+        const uint32_t b = (uint32_t)(task - S.brick_begin);   // below 2^32 within a scene
+        const uint32_t rest = fastdiv(b, S.div_nbx);
+        const uint32_t bzi = fastdiv(rest, S.div_nby);
+        const int bx0 = (int)(b - rest * (uint32_t)S.nbx) * BXV, by0 = (int)(rest - bzi * (uint32_t)S.nby) * BY,
+                  bz0 = (int)bzi * BZ;
 
         uint32_t masks[kBatchMaxFrames / 32];
         bool any = false;

@@ -155,7 +155,7 @@ def test_generate_triangular_surface_appends(gpu, oracle):
 
 
 def test_large_field_mesh_tiles_chain(gpu, oracle):
-    """A 256^3 field (about 16k tiles chained by the look-back) against the oracle."""
+    """A 256^3 field (about 16k tiles: counts, the tile scan, emission of the listed tiles) against the oracle."""
     grid = (256, 256, 256)
     tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=(2.56,) * 3, mode="fixed", max_weight=4)
     vol = TSDFVolume(tc)
