@@ -69,14 +69,14 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 
 // CTAs per SM when the caller passes 0: as many as the kernel keeps resident
 // (one wave of the persistent grid), cached per kernel.
-int integrate_default_ctas_per_sm(int mode, int arith, bool batched, int brick) {
-    static int cache[3][2][4] = {};
+int integrate_default_ctas_per_sm(int mode, int arith, int kind, int brick) {
+    static int cache[3][3][4] = {};
     const int k = mode == GBT_MODE_FIXED ? 2 : (arith == GBT_ARITH_IEEE ? 1 : 0);
     const int b = brick >= 0 && brick < 4 ? brick : 0;
-    int& n = cache[k][batched ? 1 : 0][b];
+    int& n = cache[k][kind][b];
     if (n == 0)
-        n = k == 2 ? integrate_resident_ctas_fixed(batched, b)
-                   : (k == 1 ? integrate_resident_ctas_compat_ieee(batched, b) : integrate_resident_ctas_compat_ref(batched, b));
+        n = k == 2 ? integrate_resident_ctas_fixed(kind, b)
+                   : (k == 1 ? integrate_resident_ctas_compat_ieee(kind, b) : integrate_resident_ctas_compat_ref(kind, b));
     return n;
 }
 
@@ -341,7 +341,9 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     a.div_nby = gbt::make_fastdiv(nby);
     long long grid = (long long)device_sms() *
                      (ctas_per_sm ? ctas_per_sm
-                                  : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith, false, brick));
+                                  : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith,
+                                                                       nframes <= gbt::kLaneBrickFrames ? 1 : 0,
+                                                                       brick));
     if (grid > nbricks) grid = nbricks;
     if (grid < 1) grid = 1;
     cudaError_t e;
@@ -640,7 +642,7 @@ gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_
     char* d = static_cast<char*>(b->dev);
     cudaGetLastError();  // a launch reports only its own failure
     const long long per_sm =
-        ctas_per_sm ? ctas_per_sm : gbt::integrate_default_ctas_per_sm(v0->cfg.mode, v0->cfg.arith, true, brick);
+        ctas_per_sm ? ctas_per_sm : gbt::integrate_default_ctas_per_sm(v0->cfg.mode, v0->cfg.arith, 2, brick);
     for (int w = 0; w < nwin; ++w) {
         gbt::BatchArgs a;
         std::memset(&a, 0, sizeof(a));

@@ -200,9 +200,12 @@ cudaError_t launch_weld_vertices_fixed(const WeldArgs& a, cudaStream_t s);
 // Batched integrate (one persistent launch over many volumes).
 cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 // CTAs per SM that the (batched or pass) integrate kernel of a brick shape keeps resident.
-int integrate_resident_ctas_compat_ref(bool batched, int brick);
-int integrate_resident_ctas_compat_ieee(bool batched, int brick);
-int integrate_resident_ctas_fixed(bool batched, int brick);
+// kind: 0 pass kernel culling a frame per lane, 1 pass kernel culling a brick per lane, 2 batched kernel.
+int integrate_resident_ctas_compat_ref(int kind, int brick);
+int integrate_resident_ctas_compat_ieee(int kind, int brick);
+int integrate_resident_ctas_fixed(int kind, int brick);
+// Passes of up to this many frames cull one brick per lane (more frames: one frame per lane).
+constexpr int kLaneBrickFrames = 16;
 cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 // k_util.cu: volume initialisation and the packed per-voxel transform records.
@@ -220,7 +223,7 @@ int volume_arith(const gbt_volume* v);
 void set_last_error(const char* msg);
 
 // CTAs per SM the integrate launchers use by default, and brick extents.
-int integrate_default_ctas_per_sm(int mode, int arith, bool batched, int brick);
+int integrate_default_ctas_per_sm(int mode, int arith, int kind, int brick);
 void brick_extent(int brick, int* bx, int* by, int* bz);
 
 }  // namespace gbt

@@ -288,6 +288,21 @@ __device__ __forceinline__ uint32_t warp_live_frames(const VolDesc& v, const Fra
     return __ballot_sync(0xffffffffu, live);
 }
 
+// The frames (bit f) for which the warp's sub-box of the brick at (bx0, by0,
+// bz0) may contain an updated voxel, evaluated by one lane for all nf frames.
+template <int MODE, int TX, int BY, int BZ>
+__device__ __forceinline__ uint32_t brick_live_frames(const VolDesc& v, const FrameSlot* slots, int nf,
+                                                      const BrickLayout<TX, BY, BZ>& L, int bx0, int by0, int bz0) {
+    const int xl = bx0, xh = min(bx0 + 4 * TX, v.nx) - 1;
+    const int yl = by0 + L.wy_lo, yh = min(by0 + L.wy_hi, v.ny - 1);
+    const int zl = bz0 + L.wz_lo, zh = min(bz0 + L.wz_hi, v.nz - 1);
+    uint32_t m = 0u;
+    if (yl <= yh && zl <= zh)
+        for (int f = 0; f < nf; ++f)
+            if (!box_culled<MODE>(v, slots[f], xl, xh, yl, yh, zl, zh)) m |= 1u << f;
+    return m;
+}
+
 // One frame's samples for the thread's (up to) 4 voxels: the depth under
 // each voxel, 0 where the voxel projects off the image (or, in the fixed
 // mode, lies at or in front of min_z) -- values the update skips -- and, in
@@ -533,7 +548,9 @@ __device__ __forceinline__ bool frames_in_turn(const VolDesc& v, const FrameSlot
     return dirty;
 }
 
-template <int MODE, int TX, int BY, int BZ>
+// Passes of up to kLaneBrickFrames frames (LANE_BRICKS) cull with one lane
+// per brick; longer passes with one lane per frame.
+template <int MODE, int TX, int BY, int BZ, bool LANE_BRICKS>
 __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ IntegrateArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
     static_assert(32 % TX == 0, "a warp spans whole x rows");
@@ -553,21 +570,55 @@ __global__ void __launch_bounds__(128) integrate_kernel(const __grid_constant__ 
     // division by the host's invariant divisors
     const uint32_t nbx = a.div_nbx.d, nby = a.div_nby.d;
 
-    for (uint32_t b = blockIdx.x; b < a.nbricks; b += gridDim.x) {
+    auto origin = [&](uint32_t b, int& bx0, int& by0, int& bz0) {
         const uint32_t rest = fastdiv(b, a.div_nbx);
         const uint32_t bzi = fastdiv(rest, a.div_nby);
-        const int bx0 = (int)(b - rest * nbx) * BXV, by0 = (int)(rest - bzi * nby) * BY, bz0 = (int)bzi * BZ;
-        // frames for which this warp's box may contain an updated voxel
-        const uint32_t fmask = warp_live_frames<MODE>(v, s_frame, 0, nf, L, bx0, by0, bz0);
-        if (fmask == 0u) continue;
+        bx0 = (int)(b - rest * nbx) * BXV;
+        by0 = (int)(rest - bzi * nby) * BY;
+        bz0 = (int)bzi * BZ;
+    };
+    // the warp's voxels of one brick, the frames of fmask in turn
+    auto process = [&](int bx0, int by0, int bz0, uint32_t fmask) {
         ThreadVoxels t;
-        if (!t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) continue;
-        t.load(v);
-        // frame by frame (the pipelined apply_frames costs this kernel more in
-        // occupancy than it gains; the batched kernel uses it)
-        const bool dirty = t.nvalid == 4 ? frames_in_turn<MODE, true>(v, s_frame, fmask, t, s_inv)
-                                         : frames_in_turn<MODE, false>(v, s_frame, fmask, t, s_inv);
-        if (dirty) t.store(v);
+        if (t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) {
+            t.load(v);
+            // frame by frame (the pipelined apply_frames costs this kernel
+            // more in occupancy than it gains; the batched kernel uses it)
+            const bool dirty = t.nvalid == 4 ? frames_in_turn<MODE, true>(v, s_frame, fmask, t, s_inv)
+                                             : frames_in_turn<MODE, false>(v, s_frame, fmask, t, s_inv);
+            if (dirty) t.store(v);
+        }
+    };
+    if constexpr (LANE_BRICKS) {
+        // The CTA's bricks are blockIdx.x + k * gridDim.x.  A warp takes them
+        // 32 at a time: lane l tests its warp's sub-box of the l-th brick
+        // against every frame of the pass, and the warp then visits the
+        // bricks with a live frame (warps do not wait for each other).
+        const uint64_t step = (uint64_t)gridDim.x;
+        for (uint64_t c0 = blockIdx.x; c0 < a.nbricks; c0 += 32 * step) {   // the same for the whole warp
+            const uint64_t bl = c0 + (uint64_t)L.lane * step;
+            uint32_t lane_frames = 0u;
+            if (bl < a.nbricks) {
+                int bx0, by0, bz0;
+                origin((uint32_t)bl, bx0, by0, bz0);
+                lane_frames = brick_live_frames<MODE>(v, s_frame, nf, L, bx0, by0, bz0);
+            }
+            for (uint32_t live = __ballot_sync(0xffffffffu, lane_frames != 0u); live; live &= live - 1) {
+                const int l = __ffs(live) - 1;
+                const uint32_t fmask = __shfl_sync(0xffffffffu, lane_frames, l);
+                int bx0, by0, bz0;
+                origin((uint32_t)(c0 + (uint64_t)l * step), bx0, by0, bz0);
+                process(bx0, by0, bz0, fmask);   // (no early exit: the loop shuffles)
+            }
+        }
+    } else {
+        // brick by brick; lane f tests frame f against the warp's sub-box
+        for (uint32_t b = blockIdx.x; b < a.nbricks; b += gridDim.x) {
+            int bx0, by0, bz0;
+            origin(b, bx0, by0, bz0);
+            const uint32_t fmask = warp_live_frames<MODE>(v, s_frame, 0, nf, L, bx0, by0, bz0);
+            if (fmask != 0u) process(bx0, by0, bz0, fmask);
+        }
     }
 }
 
@@ -1357,7 +1408,10 @@ __global__ void __launch_bounds__(256) weld_vertices_kernel(const __grid_constan
 // ---------------------------------------------------------------------------
 template <int MODE, int TX, int BY, int BZ>
 cudaError_t launch_integrate_shape(const IntegrateArgs& a, int grid, cudaStream_t s) {
-    integrate_kernel<MODE, TX, BY, BZ><<<grid, 128, 0, s>>>(a);
+    if (a.nframes <= kLaneBrickFrames)
+        integrate_kernel<MODE, TX, BY, BZ, true><<<grid, 128, 0, s>>>(a);
+    else
+        integrate_kernel<MODE, TX, BY, BZ, false><<<grid, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1399,19 +1453,22 @@ int resident_128(Kernel k) {
     return n > 0 ? n : 1;
 }
 
+// kind: 0 the pass kernel culling one frame per lane, 1 the pass kernel
+// culling one brick per lane, 2 the batched kernel
 template <int MODE, int TX, int BY, int BZ>
-int resident_shape(bool batched) {
-    return batched ? resident_128(integrate_batch_kernel<MODE, TX, BY, BZ, true>)
-                   : resident_128(integrate_kernel<MODE, TX, BY, BZ>);
+int resident_shape(int kind) {
+    if (kind == 2) return resident_128(integrate_batch_kernel<MODE, TX, BY, BZ, true>);
+    return kind == 1 ? resident_128(integrate_kernel<MODE, TX, BY, BZ, true>)
+                     : resident_128(integrate_kernel<MODE, TX, BY, BZ, false>);
 }
 
 template <int MODE>
-int resident_ctas_mode(bool batched, int brick) {
+int resident_ctas_mode(int kind, int brick) {
     switch (brick) {
-        case 1: return resident_shape<MODE, 4, 8, 4>(batched);
-        case 2: return resident_shape<MODE, 8, 2, 8>(batched);
-        case 3: return resident_shape<MODE, 16, 2, 4>(batched);
-        default: return resident_shape<MODE, 8, 4, 4>(batched);
+        case 1: return resident_shape<MODE, 4, 8, 4>(kind);
+        case 2: return resident_shape<MODE, 8, 2, 8>(kind);
+        case 3: return resident_shape<MODE, 16, 2, 4>(kind);
+        default: return resident_shape<MODE, 8, 4, 4>(kind);
     }
 }
 

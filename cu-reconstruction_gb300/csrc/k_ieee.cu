@@ -24,9 +24,9 @@ cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStre
     return launch_batch_mode<kFixed>(a, brick, grid, s);
 }
 
-int integrate_resident_ctas_compat_ieee(bool batched, int brick) { return resident_ctas_mode<kCompat>(batched, brick); }
+int integrate_resident_ctas_compat_ieee(int kind, int brick) { return resident_ctas_mode<kCompat>(kind, brick); }
 
-int integrate_resident_ctas_fixed(bool batched, int brick) { return resident_ctas_mode<kFixed>(batched, brick); }
+int integrate_resident_ctas_fixed(int kind, int brick) { return resident_ctas_mode<kFixed>(kind, brick); }
 
 cudaError_t launch_mc_compat_ieee(const McArgs& a, cudaStream_t s) { return launch_mc_mode<kCompat>(a, s); }
 

@@ -16,8 +16,8 @@ cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cud
     return refarith::launch_batch_mode<refarith::kCompat>(a, brick, grid, s);
 }
 
-int integrate_resident_ctas_compat_ref(bool batched, int brick) {
-    return refarith::resident_ctas_mode<refarith::kCompat>(batched, brick);
+int integrate_resident_ctas_compat_ref(int kind, int brick) {
+    return refarith::resident_ctas_mode<refarith::kCompat>(kind, brick);
 }
 
 cudaError_t launch_mc_compat_ref(const McArgs& a, cudaStream_t s) {
