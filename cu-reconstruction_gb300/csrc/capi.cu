@@ -158,6 +158,7 @@ const char* gbt_last_error(void) { return g_last_error.c_str(); }
 const char* gbt_version(void) { return "gbt-tsdf 0.1 sm_103a"; }
 
 gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume** out) {
+    gbt::TraceRange trace_("gbt_volume_create");
     if (!cfg || !out) return fail(GBT_ERR_INVALID_ARG, "cfg or out is NULL");
     *out = nullptr;
     const gbt_volume_cfg& c = *cfg;
@@ -259,10 +260,116 @@ gbt_status gbt_volume_destroy(gbt_volume* v) {
 }
 
 gbt_status gbt_volume_reset(gbt_volume* v, void* stream) {
+    gbt::TraceRange trace_("gbt_volume_reset");
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     cudaGetLastError();  // a launch reports only its own failure
     cudaError_t e = gbt::launch_volume_init(v->desc.D, v->desc.W, v->nvox, v->desc.trunc, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "volume initialisation");
+    return GBT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The volume file's header (little- or big-endian as the host writes it).
+struct VolumeFileHeader {
+    char magic[8];
+    uint32_t header_bytes;
+    uint32_t cfg_bytes;
+    int64_t nvox;
+    gbt_volume_cfg cfg;
+    unsigned char pad[GBT_VOLUME_FILE_HEADER_BYTES - 24 - sizeof(gbt_volume_cfg)];
+};
+static_assert(sizeof(VolumeFileHeader) == GBT_VOLUME_FILE_HEADER_BYTES, "256-byte header");
+
+constexpr int64_t kFileChunkFloats = 4 << 20;   // 16 MB of host staging per copy
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() {
+        if (f) std::fclose(f);
+    }
+};
+
+gbt_status grid_to_file(const float* dev, int64_t n, FILE* f, cudaStream_t s, std::vector<float>& buf,
+                        const char* path) {
+    for (int64_t i = 0; i < n; i += kFileChunkFloats) {
+        const int64_t m = std::min<int64_t>(kFileChunkFloats, n - i);
+        cudaError_t e = cudaMemcpyAsync(buf.data(), dev + i, (size_t)m * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(e, "gbt_volume_save: reading the volume");
+        if (std::fwrite(buf.data(), 4, (size_t)m, f) != (size_t)m)
+            return fail(GBT_ERR_IO, "gbt_volume_save: writing %s failed", path);
+    }
+    return GBT_OK;
+}
+
+gbt_status grid_from_file(float* dev, int64_t n, FILE* f, cudaStream_t s, std::vector<float>& buf,
+                          const char* path) {
+    for (int64_t i = 0; i < n; i += kFileChunkFloats) {
+        const int64_t m = std::min<int64_t>(kFileChunkFloats, n - i);
+        if (std::fread(buf.data(), 4, (size_t)m, f) != (size_t)m)
+            return fail(GBT_ERR_IO, "gbt_volume_load: %s ends before its grids do", path);
+        cudaError_t e = cudaMemcpyAsync(dev + i, buf.data(), (size_t)m * 4, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(e, "gbt_volume_load: writing the volume");
+    }
+    return GBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbt_status gbt_volume_save(const gbt_volume* v, const char* path, void* stream) {
+    gbt::TraceRange trace_("gbt_volume_save");
+    if (!v || !path) return fail(GBT_ERR_INVALID_ARG, "gbt_volume_save: volume or path is NULL");
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) return fail(GBT_ERR_IO, "gbt_volume_save: cannot open %s for writing", path);
+    VolumeFileHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, GBT_VOLUME_FILE_MAGIC, 8);
+    h.header_bytes = GBT_VOLUME_FILE_HEADER_BYTES;
+    h.cfg_bytes = (uint32_t)sizeof(gbt_volume_cfg);
+    h.nvox = v->nvox;
+    h.cfg = v->cfg;
+    if (std::fwrite(&h, sizeof(h), 1, fc.f) != 1) return fail(GBT_ERR_IO, "gbt_volume_save: writing %s failed", path);
+    std::vector<float> buf((size_t)std::min<int64_t>(kFileChunkFloats, std::max<int64_t>(v->nvox, 1)));
+    const cudaStream_t s = as_stream(stream);
+    gbt_status st = grid_to_file(v->desc.D, v->nvox, fc.f, s, buf, path);
+    if (st == GBT_OK) st = grid_to_file(v->desc.W, v->nvox, fc.f, s, buf, path);
+    if (st != GBT_OK) return st;
+    if (std::fflush(fc.f) != 0) return fail(GBT_ERR_IO, "gbt_volume_save: writing %s failed", path);
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_load(const char* path, void* stream, gbt_volume** out) {
+    gbt::TraceRange trace_("gbt_volume_load");
+    if (!path || !out) return fail(GBT_ERR_INVALID_ARG, "gbt_volume_load: path or out is NULL");
+    *out = nullptr;
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) return fail(GBT_ERR_IO, "gbt_volume_load: cannot open %s", path);
+    VolumeFileHeader h;
+    if (std::fread(&h, sizeof(h), 1, fc.f) != 1 || std::memcmp(h.magic, GBT_VOLUME_FILE_MAGIC, 8) != 0 ||
+        h.header_bytes != GBT_VOLUME_FILE_HEADER_BYTES || h.cfg_bytes != sizeof(gbt_volume_cfg))
+        return fail(GBT_ERR_IO, "gbt_volume_load: %s is not a volume file of this layout", path);
+    const int64_t nvox = (int64_t)h.cfg.voxel_grid_size[0] * h.cfg.voxel_grid_size[1] * h.cfg.voxel_grid_size[2];
+    if (nvox != h.nvox) return fail(GBT_ERR_IO, "gbt_volume_load: %s: voxel count does not match its grid", path);
+    gbt_volume* v = nullptr;
+    gbt_status st = gbt_volume_create(&h.cfg, stream, &v);
+    if (st != GBT_OK) return st;
+    std::vector<float> buf((size_t)std::min<int64_t>(kFileChunkFloats, std::max<int64_t>(nvox, 1)));
+    const cudaStream_t s = as_stream(stream);
+    st = grid_from_file(v->desc.D, nvox, fc.f, s, buf, path);
+    if (st == GBT_OK) st = grid_from_file(v->desc.W, nvox, fc.f, s, buf, path);
+    if (st != GBT_OK) {
+        const std::string msg = g_last_error;
+        gbt_volume_destroy(v);
+        g_last_error = msg;
+        return st;
+    }
+    *out = v;
     return GBT_OK;
 }
 
@@ -285,6 +392,7 @@ gbt_status gbt_volume_get_info(const gbt_volume* v, gbt_volume_info* info) {
 }
 
 gbt_status gbt_volume_transformation_voxels(gbt_volume* v, void* stream, void** out) {
+    gbt::TraceRange trace_("gbt_volume_transformation_voxels");
     if (!v || !out) return fail(GBT_ERR_INVALID_ARG, "volume or out is NULL");
     if (!v->tvox) {
         const size_t bytes = (size_t)v->nvox * 28;
@@ -304,6 +412,7 @@ gbt_status gbt_volume_transformation_voxels(gbt_volume* v, void* stream, void** 
 
 gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t nframes, int32_t brick,
                                int32_t ctas_per_sm, void* stream) {
+    gbt::TraceRange trace_("gbt_integrate_tuned");
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     gbt_status st = check_frames(frames, nframes);
     if (st != GBT_OK) return st;
@@ -438,6 +547,7 @@ extern "C" {
 
 gbt_status gbt_extract_mesh(gbt_volume* v, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
                             int64_t* n_tris, void* stream) {
+    gbt::TraceRange trace_("gbt_extract_mesh");
     if (!n_tris) return fail(GBT_ERR_INVALID_ARG, "n_tris is NULL");
     *n_tris = 0;
     gbt::McArgs a;
@@ -463,6 +573,7 @@ gbt_status gbt_extract_mesh(gbt_volume* v, float* verts, int32_t* tris, int64_t 
 
 gbt_status gbt_extract_mesh_async(gbt_volume* v, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
                                   int64_t* d_n_tris, void* stream) {
+    gbt::TraceRange trace_("gbt_extract_mesh_async");
     if (!d_n_tris) return fail(GBT_ERR_INVALID_ARG, "d_n_tris is NULL");
     gbt::McArgs a;
     gbt_status st = mc_prepare(v, verts, tris, cap_tris, index_base, &a);
@@ -537,6 +648,7 @@ gbt_status gbt_batch_destroy(gbt_batch* b) {
 gbt_status gbt_integrate_batch(gbt_batch* b, const gbt_batch_item* items, int32_t nitems, const gbt_frame* frames,
                                int32_t nframes, int32_t frames_per_launch, int32_t brick, int32_t ctas_per_sm,
                                void* stream) {
+    gbt::TraceRange trace_("gbt_integrate_batch");
     if (!b || !items || !frames) return fail(GBT_ERR_INVALID_ARG, "batch, items or frames is NULL");
     if (nitems < 1 || nitems > b->max_scenes) return fail(GBT_ERR_INVALID_ARG, "nitems %d outside 1..%d", nitems, b->max_scenes);
     if (nframes < 1 || nframes > b->max_frames)
@@ -721,6 +833,7 @@ extern "C" {
 gbt_status gbt_diff_forward(const gbt_diff_cfg* cfg, void* tsdf, void* weights, void* checkpoints,
                             uint32_t* signature, const void* depth, int32_t nframes, const void* rot,
                             const void* trans, void* stream) {
+    gbt::TraceRange trace_("gbt_diff_forward");
     gbt::DiffArgs a;
     gbt_status st = diff_args(cfg, nframes, &a);
     if (st != GBT_OK) return st;
@@ -743,6 +856,7 @@ gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, con
                              const void* depth, int32_t nframes, const void* rot, const void* trans,
                              void* grad_depth, double* grad_pose, void* grad_tsdf_before,
                              void* grad_weights_before, void* stream) {
+    gbt::TraceRange trace_("gbt_diff_backward");
     gbt::DiffArgs a;
     gbt_status st = diff_args(cfg, nframes, &a);
     if (st != GBT_OK) return st;
@@ -772,6 +886,7 @@ gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, con
 gbt_status gbt_extract_mesh_indexed(gbt_volume* v, float* verts, float* normals, int32_t* tris, int64_t cap_verts,
                                     int64_t cap_tris, int64_t index_base, int64_t* n_verts, int64_t* n_tris,
                                     void* stream) {
+    gbt::TraceRange trace_("gbt_extract_mesh_indexed");
     if (!n_verts || !n_tris) return fail(GBT_ERR_INVALID_ARG, "gbt_extract_mesh_indexed: n_verts or n_tris is NULL");
     *n_verts = 0;
     *n_tris = 0;

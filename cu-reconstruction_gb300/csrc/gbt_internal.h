@@ -3,10 +3,20 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/gbt_tsdf.h"
 
 namespace gbt {
+
+// A named NVTX range around an entry point of the C ABI: visible in a
+// profiler's timeline, a null call when no tool is attached.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // Volume as the kernels see it.  D and W are [nz][ny][nx], x fastest.
 struct VolDesc {

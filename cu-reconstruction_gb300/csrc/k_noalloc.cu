@@ -59,6 +59,7 @@ extern "C" {
 
 gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, int64_t cap_tris,
                                     int64_t index_base, int64_t* d_n_tris, void* stream) {
+    gbt::TraceRange trace_("gbt_extract_mesh_noalloc");
     char msg[320];
     if (!v || !d_n_tris || cap_tris < 0 || (cap_tris > 0 && (!verts || !tris))) {
         gbt::set_last_error("gbt_extract_mesh_noalloc: NULL volume/count/output or negative capacity");

@@ -241,6 +241,7 @@ gbt_status gbt_points_extract(const double camera_matrix[9], const void* depth, 
                               int32_t depth_format, float depth_scale, const uint8_t* color_rgb8,
                               int64_t color_pitch_bytes, int32_t width, int32_t height, const double pose[7],
                               int64_t start_index, gbt_point* points, int64_t capacity, void* stream) {
+    gbt::TraceRange trace_("gbt_points_extract");
     const char* fn = "gbt_points_extract";
     if (!camera_matrix || !depth || !pose || !points) return fail(GBT_ERR_INVALID_ARG, fn, "NULL argument");
     if (width <= 0 || height <= 0) return fail(GBT_ERR_INVALID_ARG, fn, "depth width/height parameters are zero");
@@ -280,6 +281,7 @@ gbt_status gbt_points_extract(const double camera_matrix[9], const void* depth, 
 }
 
 gbt_status gbt_points_transform(gbt_point* points, int64_t n, const double pose[7], void* stream) {
+    gbt::TraceRange trace_("gbt_points_transform");
     const char* fn = "gbt_points_transform";
     if (!pose || (n > 0 && !points)) return fail(GBT_ERR_INVALID_ARG, fn, "NULL argument");
     if (n <= 0) return fail(GBT_ERR_INVALID_ARG, fn, "the number of points is 0");
@@ -292,6 +294,7 @@ gbt_status gbt_points_transform(gbt_point* points, int64_t n, const double pose[
 gbt_status gbt_points_project(const gbt_point* points, int64_t n, const double camera_matrix[9], const double pose[7],
                               float* depth, int64_t depth_pitch_bytes, uint8_t* color_rgb8, int64_t color_pitch_bytes,
                               int32_t width, int32_t height, void* scratch, void* stream) {
+    gbt::TraceRange trace_("gbt_points_project");
     const char* fn = "gbt_points_project";
     if (!camera_matrix || !pose || !depth || !scratch || (n > 0 && !points))
         return fail(GBT_ERR_INVALID_ARG, fn, "NULL argument");
@@ -335,6 +338,7 @@ gbt_status gbt_points_project(const gbt_point* points, int64_t n, const double c
 
 gbt_status gbt_image_filter_if(float* image, int64_t pitch_bytes, int32_t width, int32_t height, float filter_value,
                                float set_value, void* stream) {
+    gbt::TraceRange trace_("gbt_image_filter_if");
     const char* fn = "gbt_image_filter_if";
     if (!image) return fail(GBT_ERR_INVALID_ARG, fn, "NULL image");
     if (width <= 0 || height <= 0) return fail(GBT_ERR_INVALID_ARG, fn, "width/height are zero");

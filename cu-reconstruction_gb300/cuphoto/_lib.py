@@ -17,6 +17,9 @@ GBT_ERR_CUDA = 2
 GBT_ERR_ALLOC = 3
 GBT_ERR_CAPACITY = 4
 GBT_ERR_TIMEOUT = 5
+GBT_ERR_IO = 6
+VOLUME_FILE_MAGIC = b"GBTVOL\x00\x01"
+VOLUME_FILE_HEADER_BYTES = 256
 
 MODE_COMPAT = 0
 MODE_FIXED = 1
@@ -98,6 +101,8 @@ SIGNATURES = [
     ("gbt_volume_create", C.c_int, [C.POINTER(VolumeCfg), C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_volume_destroy", C.c_int, [C.c_void_p]),
     ("gbt_volume_reset", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("gbt_volume_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
+    ("gbt_volume_load", C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_volume_get_info", C.c_int, [C.c_void_p, C.POINTER(VolumeInfo)]),
     ("gbt_volume_transformation_voxels", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_integrate", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_void_p]),

@@ -16,6 +16,7 @@ the engine's CUDA kernels through the C ABI; torch provides device memory and
 streams only.
 """
 import ctypes as C
+import os
 import sys
 from dataclasses import dataclass, field
 
@@ -75,6 +76,19 @@ class TSDFVolumeConfig:
         c.memory = {"device": L.MEMORY_DEVICE, "managed": L.MEMORY_MANAGED}[self.memory]
         return c
 
+    @classmethod
+    def from_c(cls, c):
+        return cls(voxel_grid_size=tuple(int(x) for x in c.voxel_grid_size),
+                   physical_size=tuple(float(x) for x in c.physical_size),
+                   global_offset=tuple(float(x) for x in c.global_offset), max_weight=float(c.max_weight),
+                   focal_x=float(c.focal_x), focal_y=float(c.focal_y), cx=float(c.cx), cy=float(c.cy),
+                   camera_width=int(c.camera_width), camera_height=int(c.camera_height),
+                   max_cell_size=float(c.max_cell_size),
+                   mode={L.MODE_COMPAT: "compat", L.MODE_FIXED: "fixed"}[c.mode],
+                   arith={L.ARITH_REFERENCE: "reference", L.ARITH_IEEE: "ieee"}[c.arith],
+                   truncation=float(c.truncation), max_depth=float(c.max_depth), min_z=float(c.min_z),
+                   memory={L.MEMORY_DEVICE: "device", L.MEMORY_MANAGED: "managed"}[c.memory])
+
 
 class _DeviceArray:
     """Zero-copy wrapper of a device pointer for torch.as_tensor."""
@@ -120,13 +134,34 @@ def make_frame(depth, pose, depth_scale=0.001):
 class TSDFVolume:
     """cuphoto::TSDFVolume on the engine (tsdf_volume.cuh:31-105)."""
 
-    def __init__(self, cfg: TSDFVolumeConfig, stream=None):
+    def __init__(self, cfg: TSDFVolumeConfig, stream=None, _handle=None):
         self.cfg = cfg
         self._lib = L.lib()
         self._h = C.c_void_p()
-        L.check(self._lib.gbt_volume_create(C.byref(cfg.to_c()), _stream_handle(stream), C.byref(self._h)))
+        if _handle is not None:
+            self._h = _handle
+        else:
+            L.check(self._lib.gbt_volume_create(C.byref(cfg.to_c()), _stream_handle(stream), C.byref(self._h)))
         self._info = L.VolumeInfo()
         L.check(self._lib.gbt_volume_get_info(self._h, C.byref(self._info)))
+
+    # -- checkpoint and resume (gbt_volume_save / gbt_volume_load) -------------
+    def save(self, path, stream=None):
+        """Writes the configuration and the distance and weight grids to `path`
+        (waits for `stream`)."""
+        L.check(self._lib.gbt_volume_save(self._h, os.fsencode(path), _stream_handle(stream)))
+
+    @classmethod
+    def load(cls, path, stream=None):
+        """A volume created from a file written by save(); integrating more
+        frames into it continues the saved volume exactly."""
+        with open(path, "rb") as f:
+            head = f.read(L.VOLUME_FILE_HEADER_BYTES)
+        lib = L.lib()
+        h = C.c_void_p()
+        L.check(lib.gbt_volume_load(os.fsencode(path), _stream_handle(stream), C.byref(h)))
+        cfg = TSDFVolumeConfig.from_c(L.VolumeCfg.from_buffer_copy(head[24:24 + C.sizeof(L.VolumeCfg)]))
+        return cls(cfg, _handle=h)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -33,7 +33,8 @@ typedef enum {
     GBT_ERR_CUDA = 2,          /* a CUDA runtime call failed */
     GBT_ERR_ALLOC = 3,         /* device allocation failed */
     GBT_ERR_CAPACITY = 4,      /* output buffer too small: counts are valid, output truncated */
-    GBT_ERR_TIMEOUT = 5        /* a bounded device-side wait gave up; results are invalid */
+    GBT_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up; results are invalid */
+    GBT_ERR_IO = 6             /* a file could not be opened, read or written, or is not a volume file */
 } gbt_status;
 
 typedef enum {
@@ -123,6 +124,22 @@ gbt_status gbt_volume_destroy(gbt_volume* vol);
 
 /* Re-runs setup_data (tsdf_volume.cu:227-254) on `stream`. */
 gbt_status gbt_volume_reset(gbt_volume* vol, void* stream);
+
+/* Checkpoint and resume.  No counterpart in the reference (its volume lives
+ * only in memory).  gbt_volume_save writes the volume's configuration and
+ * its distance and weight grids to the file `path`: a 256-byte header
+ * (GBT_VOLUME_FILE_MAGIC, the header size, sizeof(gbt_volume_cfg), the
+ * voxel count and the gbt_volume_cfg the volume was created with, in host
+ * byte order), then float32 distances[N] and float32 weights[N], x fastest.
+ * gbt_volume_load creates a volume from such a file; integrating further
+ * frames into it gives the same bits as integrating all of them into one
+ * volume.  Both wait for `stream` (work queued on it before the call is
+ * included).  Failures to open, read or write, or a file that is not a
+ * volume file of this layout: GBT_ERR_IO. */
+#define GBT_VOLUME_FILE_MAGIC "GBTVOL\x00\x01"
+#define GBT_VOLUME_FILE_HEADER_BYTES 256
+gbt_status gbt_volume_save(const gbt_volume* vol, const char* path, void* stream);
+gbt_status gbt_volume_load(const char* path, void* stream, gbt_volume** out);
 
 /* Replaces the accessors voxel_distances_data, voxel_weights_data,
  * voxel_grid_size, global_offset, scale_voxel_size, voxel_phys_size

@@ -163,3 +163,36 @@ def test_se3_helpers():
     np.testing.assert_allclose(c1.numpy(), c2.numpy(), atol=1e-12)
     assert checkpoint_shape(16, (2, 3, 4)) == (1, 2, 2, 3, 4)
     assert checkpoint_shape(8, (2, 3, 4))[0] == 0 and checkpoint_shape(17, (1, 1, 1))[0] == 2
+
+
+def test_volume_files_rejected_before_any_device_work(engine_lib, tmp_path):
+    """gbt_volume_save / gbt_volume_load argument and format checks."""
+    L = engine_lib
+    lib = L.lib()
+    out = C.c_void_p()
+    assert lib.gbt_volume_save(None, b"/nonexistent/x", None) == L.GBT_ERR_INVALID_ARG
+    assert lib.gbt_volume_load(None, None, C.byref(out)) == L.GBT_ERR_INVALID_ARG
+    missing = str(tmp_path / "missing.gbtv").encode()
+    assert lib.gbt_volume_load(missing, None, C.byref(out)) == L.GBT_ERR_IO
+    assert b"cannot open" in lib.gbt_last_error()
+    bad = tmp_path / "bad.gbtv"
+    bad.write_bytes(b"NOTAVOLUME" + bytes(300))
+    assert lib.gbt_volume_load(str(bad).encode(), None, C.byref(out)) == L.GBT_ERR_IO
+    assert b"not a volume file" in lib.gbt_last_error()
+    short = tmp_path / "short.gbtv"
+    short.write_bytes(L.VOLUME_FILE_MAGIC + bytes(10))
+    assert lib.gbt_volume_load(str(short).encode(), None, C.byref(out)) == L.GBT_ERR_IO
+    # a header whose voxel count disagrees with its grid
+    cfg = L.VolumeCfg()
+    cfg.voxel_grid_size[0] = cfg.voxel_grid_size[1] = cfg.voxel_grid_size[2] = 4
+    head = bytearray(L.VOLUME_FILE_HEADER_BYTES)
+    head[0:8] = L.VOLUME_FILE_MAGIC
+    head[8:12] = L.VOLUME_FILE_HEADER_BYTES.to_bytes(4, "little")
+    head[12:16] = C.sizeof(L.VolumeCfg).to_bytes(4, "little")
+    head[16:24] = (65).to_bytes(8, "little")
+    head[24:24 + C.sizeof(cfg)] = bytes(cfg)
+    mism = tmp_path / "mismatch.gbtv"
+    mism.write_bytes(bytes(head))
+    assert lib.gbt_volume_load(str(mism).encode(), None, C.byref(out)) == L.GBT_ERR_IO
+    assert b"voxel count" in lib.gbt_last_error()
+    assert not out.value

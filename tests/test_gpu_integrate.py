@@ -1,4 +1,6 @@
 """Integrate on the GPU against the CPU oracle (through the C ABI)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -149,3 +151,38 @@ def test_full_size_c1_against_oracle(gpu, oracle, mode):
     Do, Wo = oracle_run(oracle, tc, depths, seq.poses)
     assert np.array_equal(W, Wo)
     assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["compat", "fixed"])
+def test_checkpoint_and_resume_is_bit_identical(gpu, tmp_path, mode):
+    """Integrate 5 frames, save, load into a new volume, integrate 4 more:
+    the same bits as 9 frames into one volume; the loaded volume's
+    configuration is the saved one."""
+    from cuphoto import TSDFVolume
+    seq, tc = circle_case(n=64, frames=9, mode=mode, max_weight=6)
+    depths = [dev_depth(gpu, d) for d in (seq.depth_u16 if mode == "fixed" else seq.depth_m())]
+    whole = TSDFVolume(tc)
+    whole.integrate_frames(depths, seq.poses)
+    first = TSDFVolume(tc)
+    first.integrate_frames(depths[:5], seq.poses[:5])
+    path = str(tmp_path / "vol.gbtv")
+    first.save(path)
+    assert os.path.getsize(path) == 256 + 8 * 64 ** 3
+    resumed = TSDFVolume.load(path)
+    # (the file holds the float32 configuration the volume was created from)
+    assert bytes(resumed.cfg.to_c()) == bytes(tc.to_c()) and resumed.truncation == whole.truncation
+    assert np.array_equal(resumed.voxel_weights_data().cpu().numpy(), first.voxel_weights_data().cpu().numpy())
+    resumed.integrate_frames(depths[5:], seq.poses[5:])
+    gpu.cuda.synchronize()
+    assert (whole.voxel_weights_data() > 0).float().mean().item() > 0.05
+    assert np.array_equal(resumed.voxel_weights_data().cpu().numpy(), whole.voxel_weights_data().cpu().numpy())
+    assert np.array_equal(resumed.voxel_distances_data().cpu().numpy().view(np.uint32),
+                          whole.voxel_distances_data().cpu().numpy().view(np.uint32))
+    # a file cut short is refused
+    with open(path, "rb") as f:
+        data = f.read()
+    cut = tmp_path / "cut.gbtv"
+    cut.write_bytes(data[:len(data) - 4])
+    from cuphoto import _lib as L
+    with pytest.raises(L.GbtError):
+        TSDFVolume.load(str(cut))
