@@ -125,6 +125,8 @@ constexpr int kMcThreads = 256;
 __host__ __device__ constexpr int mc_cubes_per_thread(int mode) { return mode == 1 ? 4 : 8; }
 __host__ __device__ constexpr int mc_tile_cubes(int mode) { return kMcThreads * mc_cubes_per_thread(mode); }
 constexpr int kMcTileMin = kMcThreads * 4;   // the smallest tile of either mode
+constexpr int kMcSuperShift = 10;               // tiles per superblock of the tile scan: 1024
+inline int64_t mc_superblocks(int64_t ntiles) { return (ntiles + (1 << kMcSuperShift) - 1) >> kMcSuperShift; }
 
 struct McArgs {
     const float* D;
@@ -144,6 +146,8 @@ struct McArgs {
     int64_t cap;
     int64_t index_base;
     unsigned long long* status;  // [ntiles] triangles per tile, then exclusive offsets; zeroed before launch
+    unsigned long long* super;   // [ceil(ntiles / 1024)][2] triangles and tiles with triangles per
+                                 // superblock of 1024 tiles; zeroed before launch
     uint32_t* tile_list;         // [ntiles] tiles with triangles, in order
     unsigned int* nonempty;      // length of tile_list
     unsigned int* ticket;        // emission ticket, zeroed before launch

@@ -863,11 +863,22 @@ __device__ __forceinline__ void mc_load_tables(unsigned char* s_count, unsigned 
 //     x corners; the x + 1 nibble is the next lane's.  Each row's triangle
 //     counts go to the words of the tiles (mc_tile_cubes(MODE) cubes in
 //     linear cube order, words starting at 0) its cubes fall in.
-// (2) mc_scan_kernel: one CTA turns the tile counts into exclusive offsets in
-//     place, lists the tiles that have triangles, and writes the total.
+// (2) mc_scan_kernel: one CTA per superblock of 1024 tiles turns the tile
+//     counts into exclusive offsets in place and lists the tiles that have
+//     triangles, from the superblock totals the count kernel kept; the last
+//     writes the total.
 // (3) mc_emit_kernel: CTAs take listed tiles by ticket, classify the tile
 //     again, scan its counts and write its triangles from the tile's offset.
 // Triangles come out in the reference's linear cube order.
+// Adds n > 0 triangles to tile t's word and to its superblock's totals (the
+// triangles, and the tiles whose word was 0 until now).
+__device__ __forceinline__ void mc_add_tile(const McArgs& a, uint64_t t, unsigned n) {
+    const unsigned long long old = atomicAdd(a.status + t, (unsigned long long)n);
+    unsigned long long* sb = a.super + 2 * (t >> kMcSuperShift);
+    atomicAdd(sb, (unsigned long long)n);
+    if (old == 0ull) atomicAdd(sb + 1, 1ull);
+}
+
 constexpr uint32_t kMcSegCubes = 31;      // cubes per segment: 32 voxel columns
 constexpr uint32_t kMcRowsPerTask = 64;   // rows a warp walks per task
 constexpr uint32_t kMcRowBatch = 8;       // rows whose loads are in flight together
@@ -920,8 +931,8 @@ __global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_const
             const unsigned n0 = __reduce_add_sync(0xffffffffu, acc0);
             const unsigned n1 = __reduce_add_sync(0xffffffffu, acc1);
             if (lane == 0) {
-                if (n0) atomicAdd(a.status + cur, (unsigned long long)n0);
-                if (n1) atomicAdd(a.status + cur + 1, (unsigned long long)n1);
+                if (n0) mc_add_tile(a, cur, n0);
+                if (n1) mc_add_tile(a, cur + 1, n1);
             }
             acc0 = 0;
             acc1 = 0;
@@ -979,35 +990,45 @@ __global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_const
     }
 }
 
-constexpr int kMcScanThreads = 1024;
+constexpr int kMcScanThreads = 1 << kMcSuperShift;   // one thread per tile of a superblock
 
 // Exclusive offsets of the tiles (in place), the list of tiles with
-// triangles, the triangle total and the list length.  A thread takes a
-// contiguous run of tiles; its sums travel packed as (triangles << 24 |
-// tiles with triangles): at most 5 * 2^32 triangles and 2^22 tiles, so
-// neither field carries into the other.
+// triangles, the triangle total and the list length.  One CTA per superblock
+// of 1024 tiles: it sums the totals of the superblocks before it (kept by the
+// count kernel), then scans its own tiles.  Sums travel packed as (triangles
+// << 24 | tiles with triangles): at most 5 * 2^32 triangles and 2^22 tiles,
+// so neither field carries into the other.
 __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_constant__ McArgs a) {
     __shared__ unsigned long long s_part[kMcScanThreads / 32];
-    const uint32_t n = a.ntiles;
+    __shared__ unsigned long long s_prefix;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t per = (n + kMcScanThreads - 1) / kMcScanThreads;
-    const uint32_t b = min(tid * per, n), e = min(b + per, n);
-    // the thread's words are read 8 at a time, all 8 loads in flight together
-    constexpr uint32_t kBatch = 8;
-    unsigned long long own = 0;
-    for (uint32_t i = b; i < e; i += kBatch) {
-        unsigned long long c[kBatch];
+    const uint32_t sb = blockIdx.x;
+    // the superblocks before this one
+    unsigned long long pre = 0;
+    for (uint32_t k = tid; k < sb; k += kMcScanThreads) pre += (a.super[2 * k] << 24) | a.super[2 * k + 1];
 #pragma unroll
-        for (uint32_t j = 0; j < kBatch; ++j) c[j] = i + j < e ? a.status[i + j] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
+    if (lane == 0) s_part[warp] = pre;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long v = s_part[lane];
 #pragma unroll
-        for (uint32_t j = 0; j < kBatch; ++j) own += (c[j] << 24) | (c[j] != 0ull ? 1ull : 0ull);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) s_prefix = v;
     }
+    __syncthreads();
+    const unsigned long long prefix = s_prefix;
+    // this superblock's tiles, one per thread
+    const uint64_t t = (uint64_t)sb * kMcScanThreads + tid;
+    const unsigned long long c = t < a.ntiles ? a.status[t] : 0ull;
+    const unsigned long long own = (c << 24) | (c != 0ull ? 1ull : 0ull);
     unsigned long long x = own;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= (uint32_t)o) x += y;
     }
+    __syncthreads();   // s_part is reused
     if (lane == 31) s_part[warp] = x;
     __syncthreads();
     if (warp == 0) {
@@ -1021,22 +1042,12 @@ __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_co
         s_part[lane] = p - v;
     }
     __syncthreads();
-    const unsigned long long excl = s_part[warp] + x - own;
-    unsigned long long off = excl >> 24;
-    uint32_t k = (uint32_t)(excl & 0xffffffull);
-    for (uint32_t i = b; i < e; i += kBatch) {
-        unsigned long long c[kBatch];
-#pragma unroll
-        for (uint32_t j = 0; j < kBatch; ++j) c[j] = i + j < e ? a.status[i + j] : 0ull;
-#pragma unroll
-        for (uint32_t j = 0; j < kBatch; ++j) {
-            if (i + j >= e) break;
-            a.status[i + j] = off;
-            if (c[j]) a.tile_list[k++] = i + j;
-            off += c[j];
-        }
+    const unsigned long long excl = prefix + s_part[warp] + x - own;
+    if (t < a.ntiles) {
+        a.status[t] = excl >> 24;
+        if (c) a.tile_list[excl & 0xffffffull] = (uint32_t)t;
     }
-    if (tid == kMcScanThreads - 1) {
+    if (sb == gridDim.x - 1 && tid == kMcScanThreads - 1) {
         const unsigned long long all = excl + own;
         *a.total = (long long)(all >> 24);
         *a.nonempty = (unsigned)(all & 0xffffffull);
@@ -1497,7 +1508,7 @@ cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
     mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
-    mc_scan_kernel<<<1, kMcScanThreads, 0, s>>>(a);
+    mc_scan_kernel<<<(unsigned)((a.ntiles + kMcScanThreads - 1) / kMcScanThreads), kMcScanThreads, 0, s>>>(a);
     grid = (long long)sms * per_emit;
     if (grid > (long long)a.ntiles) grid = a.ntiles;
     if (grid < 1) grid = 1;

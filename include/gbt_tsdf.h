@@ -309,7 +309,7 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  * GPU (other streams, other host threads) race -- serialise them.
  * Failures are described by gbt_last_error(). */
 #define GBT_NOALLOC_SCRATCH_BYTES (2 << 20)
-#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64) / 12) * 1024)
+#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64 - 4096) / 12) * 1024)
 gbt_status gbt_extract_mesh_noalloc(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                     int64_t index_base, int64_t* d_n_tris, void* stream);
 
