@@ -106,6 +106,35 @@ def test_full_size_c1_vs_reference_kernels(gpu, ref):
     assert np.array_equal(V.view(np.uint32), Vr.view(np.uint32)) and np.array_equal(T, Tr)
 
 
+def test_full_size_c2_batched_vs_reference_kernels(gpu, ref):
+    """The benchmark's default workload: 512^3 voxels of 0.5 cm, 300 frames
+    640x480 uint16 along the helix, integrated by the batched kernel with the
+    bench's launch shape (brick 2, 64-frame windows, resident CTAs) and by
+    the reference's kernel one frame per call: bit-exact."""
+    from cuphoto.batch import BatchIntegrator
+    cam = S.Camera()
+    scene = S.make_scene(scene_id=0, n_spheres=6)
+    poses = S.helix_poses(300, seed=0)
+    frames = S.render_sequence_torch(scene, poses, cam, seed=0)            # (300, H, W) uint16 bits in int16
+    tc = TSDFVolumeConfig(**S.grid_for(512, 2.56), focal_x=cam.fx, focal_y=cam.fy, cx=cam.cx, cy=cam.cy,
+                          camera_width=cam.width, camera_height=cam.height, max_weight=128.0)
+    # the reference reads float metres: float(u16) * 0.001 rounded once, as the engine converts
+    metres = (frames.to(gpu.int32) & 0xFFFF).to(gpu.float32) * gpu.tensor(0.001, dtype=gpu.float32, device="cuda")
+    r = ref(tc)
+    for k in range(len(poses)):
+        r.integrate(metres[k].data_ptr(), metres.stride(1) * 4, metres.shape[2], metres.shape[1], poses[k])
+    Dr, Wr = r.read()
+    del metres
+    vol = TSDFVolume(tc)
+    BatchIntegrator(max_scenes=1, max_frames=300).integrate([vol], [[frames[k] for k in range(300)]], [poses],
+                                                             brick=2, ctas_per_sm=0, frames_per_launch=64)
+    gpu.cuda.synchronize()
+    W = vol.voxel_weights_data().cpu().numpy()
+    assert (Wr > 0).mean() > 0.05
+    assert np.array_equal(W, Wr)
+    assert np.array_equal(vol.voxel_distances_data().cpu().numpy().view(np.uint32), Dr.view(np.uint32))
+
+
 GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
 
 
