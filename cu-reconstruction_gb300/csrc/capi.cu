@@ -52,8 +52,8 @@ struct gbt_volume {
     bool managed;
     void* tvox;
     // marching-cubes scratch: [0,64) header (ticket u32, error i32, total i64, tiles listed u32),
-    // then two u64 totals per superblock of 1024 tiles, one u64 word per tile, and the u32 list
-    // of tiles with triangles
+    // then two u64 totals per superblock of 1024 tiles, one u64 word per tile, one bit per group
+    // of 32 cubes, and the u32 list of tiles with triangles
     void* mc_scratch;
     size_t mc_scratch_bytes;
     // shared-vertex mesh scratch: used-edge bits, word offsets, block sums, vertex count
@@ -506,7 +506,8 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     a->cap = cap;
     a->index_base = index_base;
     const size_t nsuper = (size_t)gbt::mc_superblocks(a->ntiles);
-    const size_t need = 64 + nsuper * 16 + (size_t)a->ntiles * 12;
+    const size_t nwords = (size_t)gbt::mc_group_words(ncubes);
+    const size_t need = 64 + nsuper * 16 + (size_t)a->ntiles * 12 + nwords * 4;
     if (v->mc_scratch_bytes < need) {
         if (v->mc_scratch) cudaFree(v->mc_scratch);
         v->mc_scratch = nullptr;
@@ -525,15 +526,17 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     a->nonempty = reinterpret_cast<unsigned int*>(s + 16);
     a->super = reinterpret_cast<unsigned long long*>(s + 64);
     a->status = a->super + 2 * nsuper;
-    a->tile_list = reinterpret_cast<uint32_t*>(a->status + a->ntiles);
+    a->group_bits = reinterpret_cast<uint32_t*>(a->status + a->ntiles);
+    a->tile_list = a->group_bits + nwords;
     return GBT_OK;
 }
 
 gbt_status mc_launch(gbt_volume* v, const gbt::McArgs& a, cudaStream_t s) {
     cudaGetLastError();  // a launch reports only its own failure
-    // header, superblock totals and tile words start at zero
+    // header, superblock totals, tile words and group bits start at zero
     cudaError_t e = cudaMemsetAsync(v->mc_scratch, 0,
-                                    64 + (size_t)gbt::mc_superblocks(a.ntiles) * 16 + (size_t)a.ntiles * 8, s);
+                                    64 + (size_t)gbt::mc_superblocks(a.ntiles) * 16 + (size_t)a.ntiles * 8 +
+                                        (size_t)gbt::mc_group_words(a.ncubes) * 4, s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh scratch clear");
     if (a.ntiles == 0) return GBT_OK;
     if (v->cfg.mode == GBT_MODE_FIXED)

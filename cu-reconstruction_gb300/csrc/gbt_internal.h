@@ -127,6 +127,7 @@ __host__ __device__ constexpr int mc_tile_cubes(int mode) { return kMcThreads * 
 constexpr int kMcTileMin = kMcThreads * 4;   // the smallest tile of either mode
 constexpr int kMcSuperShift = 10;               // tiles per superblock of the tile scan: 1024
 inline int64_t mc_superblocks(int64_t ntiles) { return (ntiles + (1 << kMcSuperShift) - 1) >> kMcSuperShift; }
+inline int64_t mc_group_words(int64_t ncubes) { return (ncubes + 1023) / 1024; }
 
 struct McArgs {
     const float* D;
@@ -149,6 +150,7 @@ struct McArgs {
     unsigned long long* super;   // [ceil(ntiles / 1024)][2] triangles and tiles with triangles per
                                  // superblock of 1024 tiles; zeroed before launch
     uint32_t* tile_list;         // [ntiles] tiles with triangles, in order
+    uint32_t* group_bits;        // [ceil(ncubes / 1024)] bit g: group g of 32 cubes has triangles; zeroed
     unsigned int* nonempty;      // length of tile_list
     unsigned int* ticket;        // emission ticket, zeroed before launch
     long long* total;            // triangle count out

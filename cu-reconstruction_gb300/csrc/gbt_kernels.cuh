@@ -976,6 +976,9 @@ __global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_const
             unsigned n = s_cnt[(sx & 15) | (sn & 15) << 4];
             if (!cube_ok || (MODE == kFixed && !(sx & sn & 16))) n = 0u;
             if ((c >> kShift) == cur) acc0 += n; else acc1 += n;
+            // the cube's group of 32 (linear order) has triangles: the emit
+            // kernel classifies only such groups
+            if (n) atomicOr(a.group_bits + (c >> 10), 1u << ((c >> 5) & 31u));
             lo = hi;
             lo_ok = hi_ok;
             c += cx_n;
@@ -1114,7 +1117,21 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
 
         int type[CPT];
         int incl[CPT];
-        mc_tile_types<MODE, CPT>(a, tile, tid, type, s_type);
+        // the warp's CPT consecutive groups of 32 cubes; only the groups the
+        // count kernel marked have triangles and are classified again
+        {
+            const uint64_t wbase = (uint64_t)c0 + (uint64_t)warp * (32 * CPT);
+#pragma unroll
+            for (int i = 0; i < CPT; ++i) {
+                const uint64_t g = (wbase >> 5) + i;
+                type[i] = 0;
+                if ((a.group_bits[g >> 5] >> (g & 31)) & 1u) {   // the same for the whole warp
+                    int t1[1];
+                    mc_warp_types<MODE, 1>(a, wbase + 32 * i, lane, t1, s_type);
+                    type[i] = t1[0];
+                }
+            }
+        }
 #pragma unroll
         for (int i = 0; i < CPT; ++i) {
             int n = s_count[type[i]];

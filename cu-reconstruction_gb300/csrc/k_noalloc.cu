@@ -21,8 +21,8 @@ namespace {
 
 // [0, 64): emission ticket (u32), error flag (i32), triangle total (i64),
 // tiles listed (u32); then two totals (u64) per superblock of 1024 tiles (at
-// most 4096 bytes), one word (u64) per tile (at least 1024 cubes) and the
-// list of tiles with triangles (u32 per tile).
+// most 4096 bytes), one word (u64) per tile (at least 1024 cubes), one bit
+// per group of 32 cubes and the list of tiles with triangles (u32 per tile).
 static __device__ __align__(256) unsigned char g_mesh_scratch[GBT_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
@@ -114,10 +114,12 @@ gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, 
     const size_t nsuper = (size_t)gbt::mc_superblocks(a.ntiles);
     a.super = reinterpret_cast<unsigned long long*>(s + 64);
     a.status = a.super + 2 * nsuper;
-    a.tile_list = reinterpret_cast<uint32_t*>(a.status + a.ntiles);
+    const size_t nwords = (size_t)gbt::mc_group_words(ncubes);
+    a.group_bits = reinterpret_cast<uint32_t*>(a.status + a.ntiles);
+    a.tile_list = a.group_bits + nwords;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the previous call's ticket, flags, counts and tile words must not leak into this one
-    e = cudaMemsetAsync(scratch, 0, 64 + nsuper * 16 + (size_t)a.ntiles * 8, st);
+    e = cudaMemsetAsync(scratch, 0, 64 + nsuper * 16 + (size_t)a.ntiles * 8 + nwords * 4, st);
     if (e == cudaSuccess && a.ntiles > 0) {
         if (gbt::volume_mode(v) == GBT_MODE_FIXED)
             e = gbt::launch_mc_fixed(a, st);

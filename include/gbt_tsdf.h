@@ -294,7 +294,7 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  * fails, or applications whose device memory is all owned by their own pool
  * or fixed budget.  gbt_extract_mesh may cudaMalloc scratch on a volume's
  * first mesh; this call never allocates: its scratch is one file-scope
- * device array of GBT_NOALLOC_SCRATCH_BYTES (2 MiB) that every GPU using the
+ * device array of GBT_NOALLOC_SCRATCH_BYTES (3 MiB) that every GPU using the
  * library holds until the process exits.  That limits it to volumes of at
  * most GBT_NOALLOC_MAX_CUBES cubes (a 512^3 grid fits); larger volumes get
  * GBT_ERR_INVALID_ARG.
@@ -308,8 +308,8 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  * each call clears it on `stream` first, and calls whose work overlaps on the
  * GPU (other streams, other host threads) race -- serialise them.
  * Failures are described by gbt_last_error(). */
-#define GBT_NOALLOC_SCRATCH_BYTES (2 << 20)
-#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64 - 4096) / 12) * 1024)
+#define GBT_NOALLOC_SCRATCH_BYTES (3 << 20)
+#define GBT_NOALLOC_MAX_CUBES ((int64_t)((GBT_NOALLOC_SCRATCH_BYTES - 64 - 4096) / 16) * 1024)
 gbt_status gbt_extract_mesh_noalloc(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                     int64_t index_base, int64_t* d_n_tris, void* stream);
 

@@ -69,12 +69,12 @@ def test_noalloc_mesh_matches_allocating_entry_point(gpu, mode, arith):
 
 
 def test_noalloc_rejects_volumes_beyond_its_scratch(gpu):
-    # 570^3 voxels = 569^3 cubes, above GBT_NOALLOC_MAX_CUBES (174416 tiles of 1024 cubes)
-    tc = TSDFVolumeConfig(voxel_grid_size=(570, 570, 570), physical_size=(2.85, 2.85, 2.85))
+    # 600^3 voxels = 599^3 cubes, above GBT_NOALLOC_MAX_CUBES (196348 tiles of 1024 cubes)
+    tc = TSDFVolumeConfig(voxel_grid_size=(600, 600, 600), physical_size=(3.0, 3.0, 3.0))
     vol = TSDFVolume(tc)
     lib = L.lib()
     count = gpu.zeros(1, dtype=gpu.int64, device="cuda")
     st = lib.gbt_extract_mesh_noalloc(vol.handle, None, None, 0, 0, C.c_void_p(count.data_ptr()), None)
     assert st == L.GBT_ERR_INVALID_ARG
     msg = lib.gbt_last_error().decode()
-    assert "static scratch" in msg and "178601984" in msg
+    assert "static scratch" in msg and "201060352" in msg
