@@ -740,7 +740,7 @@ def multiscene(args, torch, rank, world, local):
         table = []
         for fpl in (32, 64, 128):
             for brick in (0, 1, 2, 3):
-                for ctas in (4, 8, 16):
+                for ctas in (0, 8, 16):   # 0: as many as the kernel keeps resident
                     for v in vols:
                         v.reset()
                     batch.integrate(vols, depths, poses, brick=brick, ctas_per_sm=ctas, frames_per_launch=fpl)

@@ -76,6 +76,23 @@ class Frame(C.Structure):
     ]
 
 
+# gbt_frame as a numpy record, for filling many frame descriptors at once
+FRAME_DTYPE = None
+
+
+def frame_dtype():
+    global FRAME_DTYPE
+    if FRAME_DTYPE is None:
+        import numpy as np
+        FRAME_DTYPE = np.dtype({"names": ["depth", "pitch_bytes", "width", "height", "format", "depth_scale", "pose"],
+                                "formats": ["<u8", "<u8", "<i4", "<i4", "<i4", "<f4", ("<f8", 7)],
+                                "offsets": [Frame.depth.offset, Frame.pitch_bytes.offset, Frame.width.offset,
+                                            Frame.height.offset, Frame.format.offset, Frame.depth_scale.offset,
+                                            Frame.pose.offset],
+                                "itemsize": C.sizeof(Frame)})
+    return FRAME_DTYPE
+
+
 class DiffCfg(C.Structure):
     _fields_ = [
         ("voxel_grid_size", C.c_uint32 * 3),

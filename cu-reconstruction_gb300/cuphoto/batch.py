@@ -12,6 +12,39 @@ from . import _lib as L
 from .tsdf import _stream_handle, _torch, make_frame
 
 
+def _frame_records(depths, poses, depth_scale):
+    """gbt_frame records (numpy) for a list of (height, width) CUDA depth
+    tensors or one (frames, height, width) tensor, with one pose per frame."""
+    import numpy as np
+    torch = _torch()
+    rec = np.zeros(len(poses), L.frame_dtype())
+    if len(poses) == 0:
+        return rec
+    if torch.is_tensor(depths) and depths.dim() == 3:
+        if depths.shape[0] != len(poses):
+            raise ValueError("%d frames but %d poses" % (depths.shape[0], len(poses)))
+        first = depths[0]
+        rec["depth"] = first.data_ptr() + np.arange(len(poses), dtype=np.uint64) * (depths.stride(0) *
+                                                                                     depths.element_size())
+    else:
+        if len(depths) != len(poses):
+            raise ValueError("%d frames but %d poses" % (len(depths), len(poses)))
+        first = depths[0]
+        for d in depths:
+            if d.shape != first.shape or d.dtype != first.dtype or d.stride() != first.stride():
+                return np.concatenate([np.frombuffer(bytes(make_frame(d, p, depth_scale)), L.frame_dtype())
+                                       for d, p in zip(depths, poses)])
+        rec["depth"] = [d.data_ptr() for d in depths]
+    # one frame describes them all: format, size and pitch checks as make_frame does them
+    f = make_frame(first, poses[0], depth_scale)
+    rec["pitch_bytes"] = f.pitch_bytes
+    rec["width"], rec["height"] = f.width, f.height
+    rec["format"] = f.format
+    rec["depth_scale"] = f.depth_scale
+    rec["pose"] = np.asarray(poses, dtype=np.float64).reshape(len(poses), 7)
+    return rec
+
+
 class BatchIntegrator:
     def __init__(self, max_scenes=64, max_frames=4096):
         self._lib = L.lib()
@@ -34,15 +67,23 @@ class BatchIntegrator:
 
     def integrate(self, volumes, depth_lists, pose_lists, depth_scale=0.001, brick=0, ctas_per_sm=0,
                   frames_per_launch=L.MAX_FRAMES_PER_SCENE_PASS, stream=None):
-        items, frames = [], []
-        for vol, ds, ps in zip(volumes, depth_lists, pose_lists):
-            items.append(L.BatchItem(vol.handle.value, len(frames), len(ds)))
-            frames.extend(make_frame(d, p, depth_scale) for d, p in zip(ds, ps))
-        it = (L.BatchItem * len(items))(*items)
-        fr = (L.Frame * len(frames))(*frames)
-        self._keep = (it, fr)
-        L.check(self._lib.gbt_integrate_batch(self._h, it, len(items), fr, len(frames), int(frames_per_launch),
-                                              int(brick), int(ctas_per_sm), _stream_handle(stream)))
+        """depth_lists[i]: scene i's frames, a list of (height, width) CUDA
+        tensors (float32 metres or uint16 bits) or one (frames, height, width)
+        tensor; pose_lists[i]: one pose per frame."""
+        import numpy as np
+        items = (L.BatchItem * len(volumes))()
+        parts = []
+        n = 0
+        for k, (vol, ds, ps) in enumerate(zip(volumes, depth_lists, pose_lists)):
+            rec = _frame_records(ds, ps, depth_scale)
+            items[k] = L.BatchItem(vol.handle.value, n, len(rec))
+            parts.append(rec)
+            n += len(rec)
+        fr = np.concatenate(parts) if parts else np.zeros(0, L.frame_dtype())
+        self._keep = (items, fr)
+        L.check(self._lib.gbt_integrate_batch(self._h, items, len(volumes), fr.ctypes.data_as(C.POINTER(L.Frame)), n,
+                                              int(frames_per_launch), int(brick), int(ctas_per_sm),
+                                              _stream_handle(stream)))
 
     def integrate_streamed(self, volumes, host_frames, device_frames, pose_lists, depth_scale=0.001, brick=0,
                            ctas_per_sm=0, frames_per_launch=L.MAX_FRAMES_PER_SCENE_PASS, stream=None,
@@ -81,10 +122,9 @@ class BatchIntegrator:
                 done.record(copy_stream)
             cur.wait_event(done)
             sel = [i for i, h in enumerate(host_frames) if h.shape[0] > w0]
-            frames = [[device_frames[i][f] for f in range(w0, min(w0 + k_w, host_frames[i].shape[0]))] for i in sel]
-            self.integrate([volumes[i] for i in sel], frames, [pose_lists[i][w0:w0 + k_w] for i in sel],
-                           depth_scale=depth_scale, brick=brick, ctas_per_sm=ctas_per_sm, frames_per_launch=k_w,
-                           stream=cur)
+            self.integrate([volumes[i] for i in sel], [device_frames[i][w0:w0 + k_w] for i in sel],
+                           [pose_lists[i][w0:w0 + k_w] for i in sel], depth_scale=depth_scale, brick=brick,
+                           ctas_per_sm=ctas_per_sm, frames_per_launch=k_w, stream=cur)
         # the device buffers are also used on the copy stream
         for d in device_frames:
             d.record_stream(copy_stream)
