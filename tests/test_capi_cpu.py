@@ -196,3 +196,26 @@ def test_volume_files_rejected_before_any_device_work(engine_lib, tmp_path):
     assert lib.gbt_volume_load(str(mism).encode(), None, C.byref(out)) == L.GBT_ERR_IO
     assert b"voxel count" in lib.gbt_last_error()
     assert not out.value
+
+
+def test_bulk_frame_records_match_single_frames(engine_lib):
+    """The batch API's numpy frame records are byte-identical to the ctypes
+    gbt_frame of each frame, for a list of images and for one 3-D tensor
+    (CPU tensors: only their pointers and strides are read)."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+    from cuphoto.batch import _frame_records
+    from cuphoto.tsdf import make_frame
+    L = engine_lib
+    frames = torch.zeros((5, 48, 64), dtype=torch.int16)
+    poses = np.random.default_rng(0).normal(size=(5, 7))
+    single = b"".join(bytes(make_frame(frames[k], poses[k], 0.001)) for k in range(5))
+    assert _frame_records(frames, poses, 0.001).tobytes() == single
+    assert _frame_records([frames[k] for k in range(5)], list(poses), 0.001).tobytes() == single
+    # pitched rows and a float image among uint16 ones
+    wide = torch.zeros((48, 80), dtype=torch.float32)[:, :64]
+    mixed = _frame_records([frames[0], wide], list(poses[:2]), 0.002)
+    assert mixed["format"].tolist() == [L.DEPTH_U16, L.DEPTH_F32_M]
+    assert mixed["pitch_bytes"].tolist() == [128, 320]
+    with pytest.raises(ValueError):
+        _frame_records(frames, poses[:4], 0.001)
