@@ -91,15 +91,10 @@ __device__ __forceinline__ f2 compat_cam2(float r0, float r2, float t, f2 px, fl
 
 __device__ __forceinline__ float centre(int v, float vs, float off) { return ((float)v + 0.5f) * vs + off; }
 
-// (c * f) / z + cc as the reference's fast-math build evaluates it: the
-// approximate reciprocal of z, then one fused multiply-add.
-__device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(cz));
-    return __fmaf_rn(__fmul_rn(c, f), r, cc);
-}
-// Pixel coordinates (u, v) of two voxels from their camera coordinates; the
-// reciprocal of each z serves both.
+// Pixel coordinates (u, v) of two voxels from their camera coordinates,
+// ((c * f) / z + cc) as the reference's fast-math build evaluates it: the
+// approximate reciprocal of z (serving both u and v), then one fused
+// multiply-add.
 __device__ __forceinline__ void compat_proj2(f2 cx, f2 cy, f2 cz, float fx, float fy, float ccx, float ccy, f2& qu,
                                              f2& qv) {
     float r0, r1;
@@ -119,9 +114,6 @@ __device__ __forceinline__ float mc_lerp(float a, float b, float r) { return a +
 
 __device__ __forceinline__ float centre(int v, float vs, float off) {
     return __fmaf_rn(__fadd_rn((float)v, 0.5f), vs, off);
-}
-__device__ __forceinline__ float compat_q(float c, float f, float cz, float cc) {
-    return __fadd_rn(__fdiv_rn(__fmul_rn(c, f), cz), cc);
 }
 __device__ __forceinline__ f2 compat_q2(f2 c, float f, f2 cz, float cc) {
     const f2 m = f2_mul(c, f2_splat(f));
