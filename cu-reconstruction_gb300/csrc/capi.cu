@@ -1,6 +1,7 @@
 // C ABI of the engine (include/gbt_tsdf.h): volume lifetime, argument
 // checking, pose conversion and kernel dispatch.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -32,14 +33,15 @@ gbt_status cuda_fail(cudaError_t e, const char* what) {
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
+// SMs of the device current at the first call (the thread-safe
+// initialisation of a function-local static; every device here is alike)
 int device_sms() {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
     return sms;
 }
 
@@ -71,13 +73,17 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 // CTAs per SM when the caller passes 0: as many as the kernel keeps resident
 // (one wave of the persistent grid), cached per kernel.
 int integrate_default_ctas_per_sm(int mode, int arith, int kind, int brick) {
-    static int cache[3][3][4] = {};
+    // host threads may race to fill an entry: each computes the same value
+    static std::atomic<int> cache[3][3][4] = {};
     const int k = mode == GBT_MODE_FIXED ? 2 : (arith == GBT_ARITH_IEEE ? 1 : 0);
     const int b = brick >= 0 && brick < 4 ? brick : 0;
-    int& n = cache[k][kind][b];
-    if (n == 0)
+    std::atomic<int>& slot = cache[k][kind][b];
+    int n = slot.load(std::memory_order_relaxed);
+    if (n == 0) {
         n = k == 2 ? integrate_resident_ctas_fixed(kind, b)
                    : (k == 1 ? integrate_resident_ctas_compat_ieee(kind, b) : integrate_resident_ctas_compat_ref(kind, b));
+        slot.store(n, std::memory_order_relaxed);
+    }
     return n;
 }
 

@@ -1521,18 +1521,34 @@ int resident_ctas_mode(int kind, int brick) {
 
 // The three marching-cubes launches; the scratch words (ticket, total, list
 // length, tile words) are zero when the first starts.
+struct McGrid {
+    int sms, per_count, per_emit;
+};
+
+// SMs and resident CTAs of the count and emit kernels (thread-safe
+// initialisation of a function-local static)
 template <int MODE>
-cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
-    static int sms = 0, per_count = 0, per_emit = 0;
-    if (sms == 0) {
+const McGrid& mc_grid() {
+    static const McGrid g = [] {
+        McGrid r{1, 1, 1};
         int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_count, mc_count_kernel<MODE>, kMcThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_emit, mc_emit_kernel<MODE>, kMcThreads, 0);
-        if (per_count < 1) per_count = 1;
-        if (per_emit < 1) per_emit = 1;
-    }
+        cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r.per_count, mc_count_kernel<MODE>, kMcThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r.per_emit, mc_emit_kernel<MODE>, kMcThreads, 0);
+        cudaGetLastError();
+        if (r.sms < 1) r.sms = 1;
+        if (r.per_count < 1) r.per_count = 1;
+        if (r.per_emit < 1) r.per_emit = 1;
+        return r;
+    }();
+    return g;
+}
+
+template <int MODE>
+cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
+    const McGrid& mg = mc_grid<MODE>();
+    const int sms = mg.sms, per_count = mg.per_count, per_emit = mg.per_emit;
     // one warp per task (a segment of a cube layer, kMcRowsPerTask rows)
     const long long nseg = (a.gx - 1 + (long long)kMcSegCubes - 1) / kMcSegCubes;
     const long long nchunk = (a.gy - 1 + (long long)kMcRowsPerTask - 1) / kMcRowsPerTask;

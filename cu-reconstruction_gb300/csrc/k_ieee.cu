@@ -34,13 +34,12 @@ cudaError_t launch_mc_fixed(const McArgs& a, cudaStream_t s) { return launch_mc_
 
 namespace {
 unsigned weld_grid(int64_t n) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, m = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms < 1) sms = 1;
-    }
+        cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+        return m > 0 ? m : 1;
+    }();
     const int64_t want = (n + 255) / 256;
     const int64_t cap = (int64_t)sms * 16;
     return (unsigned)(want < 1 ? 1 : (want < cap ? want : cap));
