@@ -1117,7 +1117,8 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
             for (int i = 0; i < CPT; ++i) {
                 const uint64_t g = (wbase >> 5) + i;
                 type[i] = 0;
-                if ((a.group_bits[g >> 5] >> (g & 31)) & 1u) {   // the same for the whole warp
+                // (the last tile may run past the last cube and its group word)
+                if (g * 32 < a.ncubes && ((a.group_bits[g >> 5] >> (g & 31)) & 1u)) {   // the same for the whole warp
                     int t1[1];
                     mc_warp_types<MODE, 1>(a, wbase + 32 * i, lane, t1, s_type);
                     type[i] = t1[0];
