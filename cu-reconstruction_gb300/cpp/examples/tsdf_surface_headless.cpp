@@ -10,6 +10,7 @@
 //
 //   tsdf_surface_headless --config_path cfg.yaml --depth frame.u16
 //   tsdf_surface_headless --config_path cfg.yaml --sequence frames.u16 --poses poses.f64 --frames N [--per_pass K]
+//                         [--resume_volume in.gbtv] [--save_volume out.gbtv]
 //
 // --sequence integrates N frames with their own world-to-camera poses
 // (N x 7 doubles: qw qx qy qz tx ty tz) through the multi-frame driver.
@@ -120,7 +121,8 @@ int main(int argc, char** argv) {
                 f.depth_scale = depth_scale;
                 for (int j = 0; j < 7; ++j) f.pose[j] = p[7 * k + j];
             }
-            tsdf.reconstruct_sequence(frames, per_pass);
+            tsdf.reconstruct_sequence(frames, per_pass, arg(argc, argv, "--resume_volume", ""),
+                                      arg(argc, argv, "--save_volume", ""));
             cudaFree(d);
         }
         const auto mesh = tsdf.get_mesh();

@@ -45,8 +45,11 @@ public:
     // estimates normals with PCL, which nothing reads; both are left out here.
     void reconstruct_surface(const cudaPointCloud::Ptr cuda_pc);
 
-    // frames: device depth images; poses: world-to-camera {qw,qx,qy,qz,tx,ty,tz}
-    void reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass = 16);
+    // frames: device depth images; poses: world-to-camera {qw,qx,qy,qz,tx,ty,tz}.
+    // resume_from: a volume file (TSDFVolume::save) to continue instead of an
+    // empty volume; save_to: where to write the volume after the frames.
+    void reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass = 16,
+                              const std::string& resume_from = "", const std::string& save_to = "");
 
     void set_global_transformation(const SE3& transform);
     SE3 get_global_transformation() const;

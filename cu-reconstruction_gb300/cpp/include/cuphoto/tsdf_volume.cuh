@@ -13,6 +13,7 @@
 
 #include <array>
 #include <memory>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -101,7 +102,14 @@ public:
     gbt_volume* engine() const { return vol; }
     bool valid() const { return vol != nullptr; }
 
+    // Engine extension: checkpoint and resume (gbt_volume_save / gbt_volume_load).
+    // save() synchronises the device; load() returns nullptr (and logs) on failure.
+    bool save(const std::string& path) const;
+    static Ptr load(const std::string& path);
+
 private:
+    TSDFVolume(gbt_volume* loaded, const TSDFVolumeConfig& tsdf_cfg);
+
     TSDFVolumeConfig cfg;
     gbt_volume* vol = nullptr;
     gbt_volume_info info{};

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 
+#include "cuphoto/cp_exception.hpp"
 #include "cuphoto/marching_cubes.cuh"
 
 namespace cuphoto {
@@ -115,16 +116,22 @@ void TSDFSurface::reconstruct_surface(const cudaPointCloud::Ptr cuda_pc) {
     mesh_from(tsdf_volume);
 }
 
-void TSDFSurface::reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass) {
-    TSDFVolume tsdf_volume(build_cfg(), engine_options);
+void TSDFSurface::reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass,
+                                       const std::string& resume_from, const std::string& save_to) {
+    TSDFVolume::Ptr tsdf_volume = resume_from.empty() ? std::make_shared<TSDFVolume>(build_cfg(), engine_options)
+                                                      : TSDFVolume::load(resume_from);
+    if (!tsdf_volume || !tsdf_volume->valid())
+        throw CuPhotoException("TSDFSurface::reconstruct_sequence: no volume to integrate into");
     if (frames_per_pass < 1) frames_per_pass = 1;
     if (frames_per_pass > GBT_MAX_FRAMES_PER_PASS) frames_per_pass = GBT_MAX_FRAMES_PER_PASS;
     for (size_t s = 0; s < frames.size(); s += (size_t)frames_per_pass) {
         const i32 n = (i32)((frames.size() - s) < (size_t)frames_per_pass ? frames.size() - s : (size_t)frames_per_pass);
-        if (!tsdf_volume.integrate_frames(frames.data() + s, n)) return;
+        if (!tsdf_volume->integrate_frames(frames.data() + s, n)) return;
     }
     cudaDeviceSynchronize();
-    mesh_from(tsdf_volume);
+    if (!save_to.empty() && !tsdf_volume->save(save_to))
+        throw CuPhotoException("TSDFSurface::reconstruct_sequence: cannot save the volume to " + save_to);
+    mesh_from(*tsdf_volume);
 }
 
 }  // namespace cuphoto

@@ -60,6 +60,45 @@ TSDFVolume::TSDFVolume(const TSDFVolumeConfig& tsdf_cfg, const TSDFEngineOptions
     gbt_volume_get_info(vol, &info);
 }
 
+TSDFVolume::TSDFVolume(gbt_volume* loaded, const TSDFVolumeConfig& tsdf_cfg) : cfg(tsdf_cfg), vol(loaded) {
+    gbt_volume_get_info(vol, &info);
+}
+
+bool TSDFVolume::save(const std::string& path) const {
+    if (!vol) {
+        log_error("TSDFVolume::save() -- the volume was not created");
+        return false;
+    }
+    if (gbt_volume_save(vol, path.c_str(), nullptr) != GBT_OK) {
+        log_engine_error("TSDFVolume::save()");
+        return false;
+    }
+    return true;
+}
+
+TSDFVolume::Ptr TSDFVolume::load(const std::string& path) {
+    gbt_volume* v = nullptr;
+    gbt_volume_cfg e;
+    if (gbt_volume_load(path.c_str(), nullptr, &v) != GBT_OK || gbt_volume_get_cfg(v, &e) != GBT_OK) {
+        log_engine_error("TSDFVolume::load()");
+        if (v) gbt_volume_destroy(v);
+        return nullptr;
+    }
+    TSDFVolumeConfig c;
+    c.voxel_grid_size = dim3(e.voxel_grid_size[0], e.voxel_grid_size[1], e.voxel_grid_size[2]);
+    c.physical_size = make_float3(e.physical_size[0], e.physical_size[1], e.physical_size[2]);
+    c.global_offset = make_float3(e.global_offset[0], e.global_offset[1], e.global_offset[2]);
+    c.max_weight = e.max_weight;
+    c.focal_x = e.focal_x;
+    c.focal_y = e.focal_y;
+    c.cx = e.cx;
+    c.cy = e.cy;
+    c.camera_width = e.camera_width;
+    c.camera_height = e.camera_height;
+    c.max_cell_size = e.max_cell_size;
+    return Ptr(new TSDFVolume(v, c));
+}
+
 TSDFVolume::~TSDFVolume() {
     if (vol) gbt_volume_destroy(vol);
 }

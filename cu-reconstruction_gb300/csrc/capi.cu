@@ -380,6 +380,12 @@ gbt_status gbt_volume_load(const char* path, void* stream, gbt_volume** out) {
     return GBT_OK;
 }
 
+gbt_status gbt_volume_get_cfg(const gbt_volume* v, gbt_volume_cfg* cfg) {
+    if (!v || !cfg) return fail(GBT_ERR_INVALID_ARG, "gbt_volume_get_cfg: volume or cfg is NULL");
+    *cfg = v->cfg;
+    return GBT_OK;
+}
+
 gbt_status gbt_volume_get_info(const gbt_volume* v, gbt_volume_info* info) {
     if (!v || !info) return fail(GBT_ERR_INVALID_ARG, "volume or info is NULL");
     std::memset(info, 0, sizeof(*info));

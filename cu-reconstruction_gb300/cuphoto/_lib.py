@@ -120,6 +120,7 @@ SIGNATURES = [
     ("gbt_volume_reset", C.c_int, [C.c_void_p, C.c_void_p]),
     ("gbt_volume_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     ("gbt_volume_load", C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("gbt_volume_get_cfg", C.c_int, [C.c_void_p, C.POINTER(VolumeCfg)]),
     ("gbt_volume_get_info", C.c_int, [C.c_void_p, C.POINTER(VolumeInfo)]),
     ("gbt_volume_transformation_voxels", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_integrate", C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_int32, C.c_void_p]),

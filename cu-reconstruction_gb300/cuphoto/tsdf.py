@@ -155,13 +155,12 @@ class TSDFVolume:
     def load(cls, path, stream=None):
         """A volume created from a file written by save(); integrating more
         frames into it continues the saved volume exactly."""
-        with open(path, "rb") as f:
-            head = f.read(L.VOLUME_FILE_HEADER_BYTES)
         lib = L.lib()
         h = C.c_void_p()
         L.check(lib.gbt_volume_load(os.fsencode(path), _stream_handle(stream), C.byref(h)))
-        cfg = TSDFVolumeConfig.from_c(L.VolumeCfg.from_buffer_copy(head[24:24 + C.sizeof(L.VolumeCfg)]))
-        return cls(cfg, _handle=h)
+        c = L.VolumeCfg()
+        L.check(lib.gbt_volume_get_cfg(h, C.byref(c)))
+        return cls(TSDFVolumeConfig.from_c(c), _handle=h)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

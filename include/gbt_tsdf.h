@@ -140,6 +140,9 @@ gbt_status gbt_volume_reset(gbt_volume* vol, void* stream);
 #define GBT_VOLUME_FILE_HEADER_BYTES 256
 gbt_status gbt_volume_save(const gbt_volume* vol, const char* path, void* stream);
 gbt_status gbt_volume_load(const char* path, void* stream, gbt_volume** out);
+/* The configuration a volume was created with (for a loaded volume: the
+ * saved one). */
+gbt_status gbt_volume_get_cfg(const gbt_volume* vol, gbt_volume_cfg* cfg);
 
 /* Replaces the accessors voxel_distances_data, voxel_weights_data,
  * voxel_grid_size, global_offset, scale_voxel_size, voxel_phys_size

@@ -146,6 +146,40 @@ def test_headless_multi_frame_driver(gpu, tmp_path):
     np.testing.assert_allclose(V, v, rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.gpu
+def test_headless_checkpoint_and_resume(gpu, tmp_path):
+    """TSDFVolume::save / load through reconstruct_sequence: 7 frames, save,
+    then the other 5 into the loaded volume give the same mesh file as all 12
+    in one run; a missing checkpoint is reported, not integrated."""
+    cam = S.Camera.half()
+    seq = S.make_sequence(12, scene_id=0, camera=cam, trajectory="circle")
+    grid, phys, off = (96, 96, 96), (2.56,) * 3, (-1.28,) * 3
+    cfgp = str(tmp_path / "cfg.yaml")
+    whole, part = str(tmp_path / "whole.ply"), str(tmp_path / "resumed.ply")
+    frames, poses = seq.depth_u16.astype("<u2"), seq.poses.astype("<f8")
+
+    def run(ply, first, n, *extra):
+        write_config(cfgp, grid, phys, off, cam, ply)
+        (tmp_path / "f.u16").write_bytes(frames[first:first + n].tobytes())
+        (tmp_path / "p.f64").write_bytes(poses[first:first + n].tobytes())
+        return subprocess.run([EXAMPLE, "--config_path", cfgp, "--sequence", str(tmp_path / "f.u16"), "--poses",
+                               str(tmp_path / "p.f64"), "--frames", str(n), "--per_pass", "4", *extra],
+                              capture_output=True, text=True, timeout=120)
+
+    r = run(whole, 0, 12)
+    assert r.returncode == 0, r.stderr
+    ckpt = str(tmp_path / "vol.gbtv")
+    r = run(str(tmp_path / "first.ply"), 0, 7, "--save_volume", ckpt)
+    assert r.returncode == 0, r.stderr
+    assert os.path.getsize(ckpt) == 256 + 8 * 96 ** 3
+    r = run(part, 7, 5, "--resume_volume", ckpt)
+    assert r.returncode == 0, r.stderr
+    with open(whole, "rb") as a, open(part, "rb") as b:
+        assert a.read() == b.read()
+    r = run(str(tmp_path / "none.ply"), 7, 5, "--resume_volume", str(tmp_path / "missing.gbtv"))
+    assert r.returncode != 0 and "missing.gbtv" in r.stderr
+
+
 def test_headless_example_reports_missing_config(engine_lib, tmp_path):
     """Same failure behaviour as the reference example: a missing parameter
     file is reported and the program exits with EXIT_FAILURE (no GPU needed)."""
