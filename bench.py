@@ -83,7 +83,10 @@ def volume_cfg(args, cam, mode):
 
 
 class ClockSampler:
-    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while running."""
+    """nvidia-smi samples (every 100 ms) of SM clock and throttle reasons
+    while running.  Entering waits for nvidia-smi's first sample, so that the
+    region timed inside the block is sampled from its start; the summary
+    keeps the samples taken inside the block."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -93,21 +96,27 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.start = 0
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)
         except OSError:
             self.proc = None
+        self.start = len(self.lines)
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
+        self.first.set()
 
     def __exit__(self, *exc):
         if self.proc:
@@ -121,7 +130,9 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # a region shorter than the sampling interval keeps the sample taken
+        # just before it
+        for ln in self.lines[self.start:] if len(self.lines) > self.start else self.lines[-1:]:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 8:
                 continue

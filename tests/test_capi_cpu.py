@@ -98,6 +98,9 @@ def test_null_arguments_are_rejected(engine_lib):
     n = C.c_int64()
     assert lib.gbt_extract_mesh(None, None, None, 0, 0, C.byref(n), None) == L.GBT_ERR_INVALID_ARG
     assert lib.gbt_volume_get_info(None, None) == L.GBT_ERR_INVALID_ARG
+    cfg = L.VolumeCfg()
+    assert lib.gbt_volume_get_cfg(None, C.byref(cfg)) == L.GBT_ERR_INVALID_ARG
+    assert b"gbt_volume_get_cfg" in lib.gbt_last_error()
     assert lib.gbt_volume_destroy(None) == L.GBT_OK
 
 
