@@ -46,16 +46,24 @@ struct FrameDesc {
     float P[12];
 };
 
+// How the integrate kernels read a frame's depth samples.
+enum SlotFormat : int32_t {
+    kSlotF32 = 0,     // float metres
+    kSlotU16Fma = 1,  // uint16 x scale as one fused multiply-add (scale normal, 2^23 * scale finite)
+    kSlotU16Mul = 2,  // uint16 x scale as a conversion and a multiply (any other scale)
+};
+
 // A frame as the integrate kernels keep it in shared memory (80 bytes, five
-// 16-byte words): pose table entry, depth image and its row pitch in elements.
+// 16-byte words): pose table entry, depth image, its row pitch in elements,
+// the sample format and the depth scale in both halves of a paired-FP32
+// operand.
 struct __align__(16) FrameSlot {
     float pose[12];
     const void* depth;
     uint32_t pitch_elems;
-    float scale;
+    int32_t fmt;
+    unsigned long long scale2;
     uint32_t width, height;
-    int32_t u16;
-    int32_t pad;
 };
 static_assert(sizeof(FrameSlot) == 80, "five 16-byte words");
 

@@ -238,13 +238,51 @@ __device__ __forceinline__ void load_slot(const FrameDesc& fd, FrameSlot& s) {
         for (int k = 0; k < 12; ++k) s.pose[k] = fd.P[k];
     }
     const bool u16 = fd.fmt == GBT_DEPTH_U16;
+    // the fused form needs 2^23 * scale to be a finite normal float, so that
+    // it is exact: a biased exponent in [1, 254 - 23]
+    const uint32_t e = (__float_as_uint(fd.scale) >> 23) & 0xFFu;
     s.depth = fd.depth;
     s.pitch_elems = (uint32_t)(u16 ? (fd.pitch >> 1) : (fd.pitch >> 2));
-    s.scale = fd.scale;
+    s.fmt = !u16 ? kSlotF32 : (e >= 1u && e <= 231u) ? kSlotU16Fma : kSlotU16Mul;
+    s.scale2 = f2_splat(fd.scale).r;
     s.width = (uint32_t)fd.width;
     s.height = (uint32_t)fd.height;
-    s.u16 = u16 ? 1 : 0;
-    s.pad = 0;
+}
+
+// The thread's 4 depth samples, 0 where `in` is false.  uint16 depth becomes
+// metres as convertTo(CV_32F, depth_scale) does (rgbd_dataset.cpp:29): the
+// product raw * scale, rounded once.  In the fused form the float with the
+// bits of 2^23 OR raw is exactly 2^23 + raw, and fma(2^23 + raw, scale,
+// -2^23 * scale) is that same product before its one rounding (the bias
+// -2^23 * scale is exact); a product is 0 or at least |scale|, never
+// subnormal, so flushing subnormals changes nothing.  Two samples share one
+// paired FMA and no integer-to-float conversion is issued.
+__device__ __forceinline__ void gather_depth(const FrameSlot& fs, const bool (&in)[4], const uint32_t (&pix)[4],
+                                             float (&dv)[4]) {
+    const unsigned short* d16 = static_cast<const unsigned short*>(fs.depth);
+    const float* d32 = static_cast<const float*>(fs.depth);
+    const f2 S{fs.scale2};
+    // the format is the same for every thread of the CTA: one gather loop each
+    if (fs.fmt == kSlotU16Fma) {
+        uint32_t raw[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) raw[i] = in[i] ? (uint32_t)__ldg(d16 + pix[i]) : 0u;
+        const f2 B = f2_mul(S, f2_splat(-8388608.0f));
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            const f2 r = f2_fma(f2_pack(__uint_as_float(raw[h] | 0x4B000000u), __uint_as_float(raw[h + 1] | 0x4B000000u)),
+                                S, B);
+            dv[h] = f2_lo(r);
+            dv[h + 1] = f2_hi(r);
+        }
+    } else if (fs.fmt == kSlotU16Mul) {
+        const float scale = f2_lo(S);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dv[i] = in[i] ? u16_metres(__ldg(d16 + pix[i]), scale) : 0.f;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dv[i] = in[i] ? __ldg(d32 + pix[i]) : 0.f;
+    }
 }
 
 // The thread's place in a brick and its warp's sub-box.
@@ -309,9 +347,6 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
     // that height * pitch_elems fits 32 bits and that the pitch is a whole
     // number of elements)
     const float* pr = fs.pose;
-    const bool u16 = fs.u16 != 0;
-    const unsigned short* d16 = static_cast<const unsigned short*>(fs.depth);
-    const float* d32 = static_cast<const float*>(fs.depth);
     const uint32_t pitch_elems = fs.pitch_elems;
     const uint32_t width = fs.width, height = fs.height;
     if (MODE == kCompat) {
@@ -360,16 +395,7 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
             in[i] = i < nvalid && (uint32_t)pu[i] < width && (uint32_t)pv[i] < height;
             pix[i] = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
         }
-        // the format is the same for every thread of the CTA: one gather loop each
-        if (u16) {
-            // uint16 depth is converted as convertTo(CV_32F, depth_scale) does
-            // (rgbd_dataset.cpp:29): one float multiply
-#pragma unroll
-            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? u16_metres(__ldg(d16 + pix[i]), fs.scale) : 0.f;
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? __ldg(d32 + pix[i]) : 0.f;
-        }
+        gather_depth(fs, in, pix, dv);
     } else {
 #if !defined(GBT_REF_ARITH)
         // K [R | t] applied to voxel pairs in paired FP32 (the same rounding
@@ -400,14 +426,7 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
                 pix[i] = (uint32_t)vv * pitch_elems + (uint32_t)u;
             }
         }
-        // the format is the same for every thread of the CTA: one gather loop each
-        if (u16) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? __fmul_rn((float)__ldg(d16 + pix[i]), fs.scale) : 0.f;
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) dv[i] = in[i] ? __ldg(d32 + pix[i]) : 0.f;
-        }
+        gather_depth(fs, in, pix, dv);
 #endif
     }
 }
