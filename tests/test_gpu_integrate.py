@@ -44,6 +44,51 @@ def test_compat_ieee_zero_z_voxels_vs_oracle(gpu, oracle, k):
     assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
 
 
+def tiny_depth_case():
+    """A 32x24x32 grid of 1/64 m voxels (every size and offset exact in
+    float) whose every voxel projects into the 64x48 image of a camera
+    1.9-2.1 m away (identity rotation); voxel centres reach from world
+    z = -0.4375 up to 0.0469, layer 28 at exactly 0, so samples of any size
+    update most of the volume (compat distances are measured from world z).
+    Layer 28 reads pixel (0, 0) (world z == 0), whose raw values 2, 5, 7 make
+    the layer's distances, the samples' running average, subnormal at a
+    subnormal scale."""
+    vs = 1.0 / 64
+    n = (32, 24, 32)
+    tc = TSDFVolumeConfig(voxel_grid_size=n, physical_size=tuple(vs * k for k in n),
+                          global_offset=(-0.25, -0.1875, -28.5 * vs), focal_x=100.0, focal_y=100.0, cx=31.5,
+                          cy=23.5, camera_width=64, camera_height=48, arith="ieee")
+    rng = np.random.default_rng(11)
+    d16 = []
+    for raw00 in (2, 5, 7):
+        d = rng.integers(1, 2000, (48, 64)).astype(np.uint16)
+        d[rng.random(d.shape) < 0.05] = 0
+        d[0, 0] = raw00
+        d16.append(d)
+    poses = [np.array([1.0, 0, 0, 0, 0.0, 0.0, 2.0]), np.array([1.0, 0, 0, 0, 0.02, -0.01, 1.9]),
+             np.array([1.0, 0, 0, 0, -0.03, 0.02, 2.1])]
+    return tc, d16, poses
+
+
+@pytest.mark.parametrize("scale", [1e-39, 2.0 ** -126, 0.0125])
+@pytest.mark.parametrize("k", [1, 3])
+def test_uint16_depth_scales_vs_oracle(gpu, oracle, scale, k):
+    """uint16 depth at depth scales that take either form of the sample
+    conversion: a subnormal scale (the conversion and multiply), the smallest
+    normal scale and an ordinary one (the fused form): bit-exact against the
+    oracle's float32 products, subnormal distances included."""
+    tc, d16, poses = tiny_depth_case()
+    _, D, W = engine_run(gpu, tc, d16, poses, k=k, depth_scale=scale)
+    Do, Wo = oracle_run(oracle, tc, d16, poses, depth_scale=scale)
+    assert (Wo > 0).mean() > 0.5
+    assert np.array_equal(W, Wo)
+    assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
+    if scale < 1e-30:
+        # distances near world z == 0 average subnormal samples
+        tiny = (Do != 0) & (np.abs(Do) < np.finfo(np.float32).tiny)
+        assert tiny.any()
+
+
 @pytest.mark.parametrize("fmt", ["u16", "f32"])
 @pytest.mark.parametrize("k", [1, 5, 32])
 @pytest.mark.parametrize("case", ["circle", "odd"])
