@@ -1090,12 +1090,12 @@ def main():
     # The kernel is bound by instruction issue, not by HBM (a window of K
     # frames shares each voxel's 16 bytes).  Its issue roofline: warp
     # instructions per voxel-update from one ncu capture of this kernel (320^3,
-    # 64-frame window: 1.675 G warp instructions for 2.097 G updates), times
+    # 64-frame window: 1.604 G warp instructions for 2.097 G updates), times
     # the measured update rate, against one instruction per clock on each of
     # the 4 schedulers of every SM at the median SM clock sampled while timing.
     issue = None
     if path == "batched" and args.mode == "compat":
-        warp_inst_per_update = 1.675292e9 / (320 ** 3 * 64)
+        warp_inst_per_update = 1.604319e9 / (320 ** 3 * 64)
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         sm_mhz = (clocks.summary().get("sm_mhz") or 0.0)
         upd_per_s = nvox * (nf / n_passes) / (launch_ms * 1e-3)

@@ -372,12 +372,13 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
             cz2[h >> 1] = czv;
         }
         // A voxel with world z == 0 or camera z == 0 maps to pixel (0, 0).
-        // One product tests the thread's 5 z values: it is 0 or NaN whenever a
-        // factor is 0 (0 * finite = 0, 0 * inf = 0 * NaN = NaN), and a product
-        // that is 0 or NaN for any other reason (underflow, a NaN factor) only
-        // sends the thread through the per-voxel test.
+        // World z is the thread's own (one comparison, out of the frame
+        // loop); one product tests the 4 camera z values: it is 0 or NaN
+        // whenever a factor is 0 (0 * finite = 0, 0 * inf = 0 * NaN = NaN),
+        // and a product that is 0 or NaN for any other reason (underflow, a
+        // NaN factor) only sends the thread through the per-voxel test.
         const f2 zz = f2_mul(cz2[0], cz2[1]);
-        if (!(fabsf(__fmul_rn(__fmul_rn(f2_lo(zz), f2_hi(zz)), pz)) > 0.f)) {
+        if (pz == 0.f || !(fabsf(__fmul_rn(f2_lo(zz), f2_hi(zz))) > 0.f)) {
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const float cz = (i & 1) ? f2_hi(cz2[i >> 1]) : f2_lo(cz2[i >> 1]);
@@ -480,31 +481,32 @@ __device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)
 
 // Applies the frames of `mask` (bit f: slots[f]) in order to the thread's
 // voxels, the next frame's samples gathered before the current frame's
-// update; returns whether any voxel changed.
+// update; returns whether any voxel changed.  The loop body covers two
+// frames, the two sample sets taking turns as the one gathered and the one
+// applied, so that no copy from one to the other is issued.
 template <int MODE, bool FULL>
 __device__ __forceinline__ bool apply_frames(const VolDesc& v, const FrameSlot* slots, uint32_t mask, const float* px,
                                              float py, float pz, int nvalid, float* d, float* w, const float* s_inv) {
     if (!mask) return false;
     bool dirty = false;
-    float dv[4], zc[4];
-    int f = __ffs(mask) - 1;
+    float dva[4], zca[4], dvb[4], zcb[4];
+    frame_samples<MODE, FULL>(v, slots[__ffs(mask) - 1], px, py, pz, nvalid, dva, zca);
     mask &= mask - 1;
-    frame_samples<MODE, FULL>(v, slots[f], px, py, pz, nvalid, dv, zc);
     for (;;) {
-        float dvn[4], zcn[4];
-        const bool more = mask != 0u;
+        bool more = mask != 0u;
         if (more) {
-            f = __ffs(mask) - 1;
+            frame_samples<MODE, FULL>(v, slots[__ffs(mask) - 1], px, py, pz, nvalid, dvb, zcb);
             mask &= mask - 1;
-            frame_samples<MODE, FULL>(v, slots[f], px, py, pz, nvalid, dvn, zcn);
         }
-        dirty |= frame_update<MODE, FULL>(v, dv, zc, pz, nvalid, d, w, s_inv);
+        dirty |= frame_update<MODE, FULL>(v, dva, zca, pz, nvalid, d, w, s_inv);
         if (!more) break;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            dv[i] = dvn[i];
-            zc[i] = zcn[i];
+        more = mask != 0u;
+        if (more) {
+            frame_samples<MODE, FULL>(v, slots[__ffs(mask) - 1], px, py, pz, nvalid, dva, zca);
+            mask &= mask - 1;
         }
+        dirty |= frame_update<MODE, FULL>(v, dvb, zcb, pz, nvalid, d, w, s_inv);
+        if (!more) break;
     }
     return dirty;
 }

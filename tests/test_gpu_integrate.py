@@ -83,8 +83,8 @@ def test_uint16_depth_scales_vs_oracle(gpu, oracle, scale, k):
     assert (Wo > 0).mean() > 0.5
     assert np.array_equal(W, Wo)
     assert np.array_equal(D.view(np.uint32), Do.view(np.uint32))
-    if scale < 1e-30:
-        # distances near world z == 0 average subnormal samples
+    if scale < 2.0 ** -126:
+        # a subnormal scale: layer 28 averages subnormal samples
         tiny = (Do != 0) & (np.abs(Do) < np.finfo(np.float32).tiny)
         assert tiny.any()
 
