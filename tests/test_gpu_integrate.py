@@ -126,15 +126,18 @@ def test_compat_reference_arith_vs_oracle(gpu, oracle, case):
     assert n_flip <= max(20, 2e-3 * D.size)
 
 
+@pytest.mark.parametrize("k", [16, 24])
 @pytest.mark.parametrize("mode", ["compat", "fixed"])
 @pytest.mark.parametrize("brick", [0, 1, 2, 3])
-def test_fused_pass_equals_per_frame_passes(gpu, mode, brick):
+def test_fused_pass_equals_per_frame_passes(gpu, mode, brick, k):
     """Frames fused in one pass give bit-identical volumes to one pass per
-    frame, for every brick shape (full-size-independent property)."""
-    seq, tc = circle_case(n=96, frames=16, mode=mode, max_weight=8)
+    frame, for every brick shape and both forms of the pass kernel (16
+    frames: a lane per brick culls, frame by frame; 24: a lane per frame
+    culls, the next frame's samples gathered during the current update)."""
+    seq, tc = circle_case(n=96, frames=k, mode=mode, max_weight=8)
     depths = list(seq.depth_u16) if mode == "fixed" else list(seq.depth_m())
     _, D1, W1 = engine_run(gpu, tc, depths, seq.poses, k=1, brick=brick)
-    _, D2, W2 = engine_run(gpu, tc, depths, seq.poses, k=16, brick=brick, ctas_per_sm=3)
+    _, D2, W2 = engine_run(gpu, tc, depths, seq.poses, k=k, brick=brick, ctas_per_sm=3)
     assert np.array_equal(W1, W2) and np.array_equal(D1.view(np.uint32), D2.view(np.uint32))
 
 
