@@ -131,6 +131,14 @@ void fixed_projection(const double* pose, const gbt_volume_cfg& c, float* P) {
     P[11] = (float)t[2];
 }
 
+// Voxels of a grid, or -1 when there are 2^32 or more (no intermediate
+// product overflows: n0 * n1 < 2^64).
+int64_t grid_voxels(const uint32_t n[3]) {
+    const uint64_t n01 = (uint64_t)n[0] * n[1];
+    if (n[2] != 0 && n01 > 0xffffffffull / n[2]) return -1;
+    return (int64_t)(n01 * n[2]);
+}
+
 gbt_status check_frames(const gbt_frame* frames, int32_t nframes) {
     if (!frames) return fail(GBT_ERR_INVALID_ARG, "frames is NULL");
     if (nframes < 1 || nframes > GBT_MAX_FRAMES_PER_PASS)
@@ -177,8 +185,8 @@ gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume
         if (c.voxel_grid_size[i] > (1u << 24))
             return fail(GBT_ERR_INVALID_ARG, "voxel_grid_size[%d] above 2^24", i);
     }
-    const int64_t nvox = (int64_t)c.voxel_grid_size[0] * c.voxel_grid_size[1] * c.voxel_grid_size[2];
-    if (nvox >= (int64_t)1 << 32) return fail(GBT_ERR_INVALID_ARG, "volume has %lld voxels; limit is 2^32-1", (long long)nvox);
+    const int64_t nvox = grid_voxels(c.voxel_grid_size);
+    if (nvox < 0) return fail(GBT_ERR_INVALID_ARG, "volume has 2^32 or more voxels; limit is 2^32-1");
     if (c.mode != GBT_MODE_COMPAT && c.mode != GBT_MODE_FIXED) return fail(GBT_ERR_INVALID_ARG, "unknown mode %d", c.mode);
     if (c.arith != GBT_ARITH_REFERENCE && c.arith != GBT_ARITH_IEEE)
         return fail(GBT_ERR_INVALID_ARG, "unknown arith %d", c.arith);
@@ -361,8 +369,9 @@ gbt_status gbt_volume_load(const char* path, void* stream, gbt_volume** out) {
     if (std::fread(&h, sizeof(h), 1, fc.f) != 1 || std::memcmp(h.magic, GBT_VOLUME_FILE_MAGIC, 8) != 0 ||
         h.header_bytes != GBT_VOLUME_FILE_HEADER_BYTES || h.cfg_bytes != sizeof(gbt_volume_cfg))
         return fail(GBT_ERR_IO, "gbt_volume_load: %s is not a volume file of this layout", path);
-    const int64_t nvox = (int64_t)h.cfg.voxel_grid_size[0] * h.cfg.voxel_grid_size[1] * h.cfg.voxel_grid_size[2];
-    if (nvox != h.nvox) return fail(GBT_ERR_IO, "gbt_volume_load: %s: voxel count does not match its grid", path);
+    const int64_t nvox = grid_voxels(h.cfg.voxel_grid_size);
+    if (nvox < 0 || nvox != h.nvox)
+        return fail(GBT_ERR_IO, "gbt_volume_load: %s: voxel count does not match its grid", path);
     gbt_volume* v = nullptr;
     gbt_status st = gbt_volume_create(&h.cfg, stream, &v);
     if (st != GBT_OK) return st;
@@ -816,8 +825,8 @@ gbt_status diff_args(const gbt_diff_cfg* c, int32_t nframes, gbt::DiffArgs* a) {
     for (int i = 0; i < 3; ++i)
         if (c->voxel_grid_size[i] == 0 || !(c->voxel_size[i] > 0.f))
             return fail(GBT_ERR_INVALID_ARG, "grid/voxel size %d must be positive", i);
-    const int64_t n = (int64_t)c->voxel_grid_size[0] * c->voxel_grid_size[1] * c->voxel_grid_size[2];
-    if (n >= (int64_t)1 << 32) return fail(GBT_ERR_INVALID_ARG, "more than 2^32-1 voxels");
+    const int64_t n = grid_voxels(c->voxel_grid_size);
+    if (n < 0) return fail(GBT_ERR_INVALID_ARG, "more than 2^32-1 voxels");
     if (!(c->truncation > 0.f) || !(c->max_weight > 0.f) || !(c->max_depth > 0.f))
         return fail(GBT_ERR_INVALID_ARG, "truncation, max_depth and max_weight must be > 0");
     if (c->width < 2 || c->height < 2) return fail(GBT_ERR_INVALID_ARG, "depth images need at least 2x2 pixels");

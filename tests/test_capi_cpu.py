@@ -78,6 +78,8 @@ def _cfg(L, **kw):
     (dict(memory=2), "unknown memory"),
     (dict(mode=1, max_weight=0.0), "max_weight"),
     (dict(voxel_grid_size=(2048, 2048, 1024)), "limit is 2^32-1"),
+    # a product of 2^72: rejected without an overflowing multiplication
+    (dict(voxel_grid_size=(1 << 24, 1 << 24, 1 << 24)), "limit is 2^32-1"),
 ])
 def test_volume_create_rejects_bad_config(engine_lib, kw, msg):
     L = engine_lib
@@ -197,6 +199,15 @@ def test_volume_files_rejected_before_any_device_work(engine_lib, tmp_path):
     mism = tmp_path / "mismatch.gbtv"
     mism.write_bytes(bytes(head))
     assert lib.gbt_volume_load(str(mism).encode(), None, C.byref(out)) == L.GBT_ERR_IO
+    assert b"voxel count" in lib.gbt_last_error()
+    # a grid of 2^64 voxels, whose count wraps to the header's 0 in 64 bits
+    cfg.voxel_grid_size[0] = cfg.voxel_grid_size[1] = 1 << 22
+    cfg.voxel_grid_size[2] = 1 << 20
+    head[16:24] = (0).to_bytes(8, "little")
+    head[24:24 + C.sizeof(cfg)] = bytes(cfg)
+    huge = tmp_path / "huge.gbtv"
+    huge.write_bytes(bytes(head))
+    assert lib.gbt_volume_load(str(huge).encode(), None, C.byref(out)) == L.GBT_ERR_IO
     assert b"voxel count" in lib.gbt_last_error()
     assert not out.value
 
