@@ -502,6 +502,9 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     if (cap < 0) return fail(GBT_ERR_INVALID_ARG, "negative capacity");
     if (cap > 0 && ((!verts && !indexed) || !tris)) return fail(GBT_ERR_INVALID_ARG, "output buffers are NULL");
+    if (!indexed && !gbt::mc_indices_fit(cap, index_base))
+        return fail(GBT_ERR_INVALID_ARG, "index_base %lld + 3 x %lld triangles passes the int32 index range",
+                    (long long)index_base, (long long)cap);
     const gbt::VolDesc& d = v->desc;
     std::memset(a, 0, sizeof(*a));
     a->D = d.D;

@@ -136,6 +136,14 @@ constexpr int kMcTileMin = kMcThreads * 4;   // the smallest tile of either mode
 constexpr int kMcSuperShift = 10;               // tiles per superblock of the tile scan: 1024
 inline int64_t mc_superblocks(int64_t ntiles) { return (ntiles + (1 << kMcSuperShift) - 1) >> kMcSuperShift; }
 inline int64_t mc_group_words(int64_t ncubes) { return (ncubes + 1023) / 1024; }
+// Triangle t of a mesh without shared vertices has the int32 indices
+// index_base + 3t, +1, +2: a capacity whose last index would pass
+// INT32_MAX, or a negative base, is refused before anything is written
+// (a count-only call, capacity 0, is always accepted).
+inline bool mc_indices_fit(int64_t cap_tris, int64_t index_base) {
+    return cap_tris == 0 ||
+           (index_base >= 0 && index_base <= INT32_MAX && cap_tris <= ((int64_t)INT32_MAX + 1 - index_base) / 3);
+}
 
 struct McArgs {
     const float* D;

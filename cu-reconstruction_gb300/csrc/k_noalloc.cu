@@ -66,6 +66,10 @@ gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, 
         gbt::set_last_error("gbt_extract_mesh_noalloc: NULL volume/count/output or negative capacity");
         return GBT_ERR_INVALID_ARG;
     }
+    if (!gbt::mc_indices_fit(cap_tris, index_base)) {
+        gbt::set_last_error("gbt_extract_mesh_noalloc: index_base + 3 x cap_tris passes the int32 index range");
+        return GBT_ERR_INVALID_ARG;
+    }
     const gbt::VolDesc& d = *gbt::volume_desc(v);
     const int64_t ncubes =
         (d.nx >= 2 && d.ny >= 2 && d.nz >= 2) ? (int64_t)(d.nx - 1) * (d.ny - 1) * (d.nz - 1) : 0;

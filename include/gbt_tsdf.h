@@ -265,7 +265,10 @@ gbt_status gbt_diff_backward(const gbt_diff_cfg* cfg, const void* grad_tsdf, con
  * Triangles come out in the reference's order: cube z, y, x, then table order.
  * Synchronises `stream`.  Returns GBT_ERR_CAPACITY if the count exceeds cap_tris
  * (the first cap_tris triangles are still written).  verts/tris may be NULL
- * when cap_tris is 0 (count only). */
+ * when cap_tris is 0 (count only).  With cap_tris > 0 the indices must fit
+ * int32: index_base >= 0 and index_base + 3 * cap_tris <= 2^31, else
+ * GBT_ERR_INVALID_ARG before anything is written (also for the _async and
+ * _noalloc forms). */
 gbt_status gbt_extract_mesh(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris, int64_t index_base,
                             int64_t* n_tris, void* stream);
 

@@ -106,6 +106,23 @@ def test_null_arguments_are_rejected(engine_lib):
     assert lib.gbt_volume_destroy(None) == L.GBT_OK
 
 
+def test_mesh_index_range_is_checked_first(engine_lib):
+    """A capacity whose int32 triangle indices would pass INT32_MAX, or a
+    negative index base, is refused before the volume handle is used (the
+    handle here is a placeholder the library never reads)."""
+    L = engine_lib
+    lib = L.lib()
+    fake = C.create_string_buffer(4096)
+    buf = C.create_string_buffer(64)
+    n = C.c_int64()
+    # (2^29 triangles from 2^29 end exactly at INT32_MAX; one more passes it)
+    for cap, base in [(1, 2 ** 31 - 2), (2, -1), (2 ** 29 + 1, 2 ** 29)]:
+        st = lib.gbt_extract_mesh(C.cast(fake, C.c_void_p), buf, buf, cap, base, C.byref(n), None)
+        assert st == L.GBT_ERR_INVALID_ARG and b"int32" in lib.gbt_last_error()
+        st = lib.gbt_extract_mesh_noalloc(C.cast(fake, C.c_void_p), buf, buf, cap, base, buf, None)
+        assert st == L.GBT_ERR_INVALID_ARG and b"int32" in lib.gbt_last_error()
+
+
 def test_diff_rejects_bad_arguments(engine_lib):
     """Argument checks of the differentiable entry points run before any
     device work (no GPU needed)."""

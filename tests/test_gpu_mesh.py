@@ -101,6 +101,17 @@ def test_capacity_and_count_only(gpu, oracle):
     assert st == L.GBT_ERR_CAPACITY and n.value == total
     Vo, To = oracle.mc_compat(oracle.cfg_from(tc), D.ravel())
     assert np.array_equal(Vb.cpu().numpy(), Vo[:cap]) and np.array_equal(Tb.cpu().numpy(), To[:cap])
+    # int32 indices: one triangle from 2^31 - 3 ends at INT32_MAX; from 2^31 - 2
+    # it would pass it, and nothing is written
+    st = lib.gbt_extract_mesh(vol.handle, C.c_void_p(Vb.data_ptr()), C.c_void_p(Tb.data_ptr()), 1, 2 ** 31 - 3,
+                              C.byref(n), None)
+    assert st == L.GBT_ERR_CAPACITY and n.value == total
+    assert Tb[0].tolist() == [2 ** 31 - 3, 2 ** 31 - 2, 2 ** 31 - 1]
+    Tb.zero_()
+    st = lib.gbt_extract_mesh(vol.handle, C.c_void_p(Vb.data_ptr()), C.c_void_p(Tb.data_ptr()), 1, 2 ** 31 - 2,
+                              C.byref(n), None)
+    assert st == L.GBT_ERR_INVALID_ARG and b"int32" in lib.gbt_last_error()
+    assert int(Tb.abs().sum().item()) == 0
 
 
 def test_async_count_and_index_base(gpu, oracle):
