@@ -255,6 +255,7 @@ gbt_status gbt_points_extract(const double camera_matrix[9], const void* depth, 
         return fail(GBT_ERR_INVALID_ARG, fn, "colour pitch below the row size");
     if (start_index < 0 || capacity < 0) return fail(GBT_ERR_INVALID_ARG, fn, "negative start index or capacity");
     const int64_t npix = (int64_t)width * height;
+    if (npix > (int64_t)0xffffffffll) return fail(GBT_ERR_INVALID_ARG, fn, "image larger than 2^32-1 pixels");
     if (start_index > capacity - npix)
         return fail(GBT_ERR_CAPACITY, fn, "start_index + width*height exceeds the cloud's capacity");
     if (!(camera_matrix[0] != 0.0) || !(camera_matrix[4] != 0.0))
@@ -285,6 +286,7 @@ gbt_status gbt_points_transform(gbt_point* points, int64_t n, const double pose[
     const char* fn = "gbt_points_transform";
     if (!pose || (n > 0 && !points)) return fail(GBT_ERR_INVALID_ARG, fn, "NULL argument");
     if (n <= 0) return fail(GBT_ERR_INVALID_ARG, fn, "the number of points is 0");
+    if (n > (int64_t)0xffffffffll) return fail(GBT_ERR_INVALID_ARG, fn, "point count above 2^32-1");
     cudaGetLastError();
     transform_kernel<<<blocks_for(n), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
         reinterpret_cast<unsigned char*>(points), n, make_pose(pose));

@@ -133,6 +133,11 @@ def test_points_entry_points_reject_bad_arguments(engine_lib):
     st = lib.gbt_points_extract(C.byref(K), dev, 256, 7, 0.001, None, 0, 64, 48, C.byref(P), 0, dev, 3072, None)
     assert st == L.GBT_ERR_INVALID_ARG
     assert lib.gbt_points_transform(dev, 0, C.byref(P), None) == L.GBT_ERR_INVALID_ARG
+    # counts that one launch's 32-bit block numbering does not cover
+    assert lib.gbt_points_transform(dev, 1 << 33, C.byref(P), None) == L.GBT_ERR_INVALID_ARG
+    st = lib.gbt_points_extract(C.byref(K), dev, 1 << 20, L.DEPTH_F32_M, 0.001, None, 0, 1 << 18, 1 << 15, C.byref(P),
+                                0, dev, 1 << 40, None)
+    assert st == L.GBT_ERR_INVALID_ARG and b"2^32" in lib.gbt_last_error()
     st = lib.gbt_points_project(dev, 10, C.byref(K), C.byref(P), dev, 256, None, 0, 64, 48, None, None)
     assert st == L.GBT_ERR_INVALID_ARG   # no scratch
     st = lib.gbt_points_project(dev, 1 << 33, C.byref(K), C.byref(P), dev, 256, None, 0, 64, 48, dev, None)
