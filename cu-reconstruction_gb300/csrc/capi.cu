@@ -825,9 +825,12 @@ namespace {
 gbt_status diff_args(const gbt_diff_cfg* c, int32_t nframes, gbt::DiffArgs* a) {
     if (!c) return fail(GBT_ERR_INVALID_ARG, "cfg is NULL");
     if (c->dtype != 0 && c->dtype != 1) return fail(GBT_ERR_INVALID_ARG, "dtype %d is not 0 or 1", c->dtype);
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
         if (c->voxel_grid_size[i] == 0 || !(c->voxel_size[i] > 0.f))
             return fail(GBT_ERR_INVALID_ARG, "grid/voxel size %d must be positive", i);
+        // (the kernels keep each extent in 32-bit signed integers)
+        if (c->voxel_grid_size[i] > (1u << 24)) return fail(GBT_ERR_INVALID_ARG, "voxel_grid_size[%d] above 2^24", i);
+    }
     const int64_t n = grid_voxels(c->voxel_grid_size);
     if (n < 0) return fail(GBT_ERR_INVALID_ARG, "more than 2^32-1 voxels");
     if (!(c->truncation > 0.f) || !(c->max_weight > 0.f) || !(c->max_depth > 0.f))

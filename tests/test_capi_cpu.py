@@ -147,6 +147,11 @@ def test_diff_rejects_bad_arguments(engine_lib):
     c.dtype = 0
     c.truncation = 0.0
     assert lib.gbt_diff_forward(C.byref(c), p, p, None, None, p, 1, p, p, None) == L.GBT_ERR_INVALID_ARG
+    c.truncation = 0.03
+    # one axis of 2^31 + 5 voxels: fewer than 2^32 in all, but not a 32-bit signed extent
+    c.voxel_grid_size[0], c.voxel_grid_size[1], c.voxel_grid_size[2] = (1 << 31) + 5, 1, 1
+    assert lib.gbt_diff_forward(C.byref(c), p, p, None, None, p, 1, p, p, None) == L.GBT_ERR_INVALID_ARG
+    assert b"above 2^24" in lib.gbt_last_error()
 
 
 def test_se3_helpers():
