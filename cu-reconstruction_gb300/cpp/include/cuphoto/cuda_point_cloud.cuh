@@ -42,6 +42,9 @@ public:
     using Ptr = std::shared_ptr<cudaPointCloud>;
 
     ~cudaPointCloud();
+    // the cloud owns its device buffer: shared through Ptr, never copied
+    cudaPointCloud(const cudaPointCloud&) = delete;
+    cudaPointCloud& operator=(const cudaPointCloud&) = delete;
 
     static cudaPointCloud::Ptr create(const std::array<r64, 9>& camera_mat, const size_t total_number_pts);
 
