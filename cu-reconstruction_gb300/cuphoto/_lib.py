@@ -186,3 +186,26 @@ def check(status):
     if status != GBT_OK:
         raise GbtError(status, lib().gbt_last_error().decode())
     return status
+
+
+def device_tensor(t, name):
+    """`t`, after checking that it lives in CUDA memory: the library reads and
+    writes the pointers it is given on the GPU, where a host address faults."""
+    if not getattr(t, "is_cuda", False):
+        raise ValueError("%s must be a CUDA tensor (got %s)" % (name, getattr(t, "device", type(t).__name__)))
+    return t
+
+
+def device_image(t, name, dtypes, channels=0):
+    """`t` as an image the kernels address by rows: a CUDA tensor of one of
+    `dtypes`, (H, W) or, with `channels`, (H, W, channels), its pixels (and
+    their channels) adjacent within a row; rows may be pitched."""
+    device_tensor(t, name)
+    if t.dtype not in dtypes:
+        raise TypeError("%s must be %s, got %s" % (name, " or ".join(str(d) for d in dtypes), t.dtype))
+    if channels:
+        if t.dim() != 3 or t.shape[2] != channels or t.stride(2) != 1 or t.stride(1) != channels:
+            raise ValueError("%s must be (H, W, %d) with interleaved channels" % (name, channels))
+    elif t.dim() != 2 or t.stride(1) != 1:
+        raise ValueError("%s must be (H, W) with contiguous rows" % name)
+    return t

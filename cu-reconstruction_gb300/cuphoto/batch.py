@@ -23,6 +23,7 @@ def _frame_records(depths, poses, depth_scale):
     if torch.is_tensor(depths) and depths.dim() == 3:
         if depths.shape[0] != len(poses):
             raise ValueError("%d frames but %d poses" % (depths.shape[0], len(poses)))
+        L.device_tensor(depths, "depths")
         first = depths[0]
         rec["depth"] = first.data_ptr() + np.arange(len(poses), dtype=np.uint64) * (depths.stride(0) *
                                                                                      depths.element_size())
@@ -31,6 +32,7 @@ def _frame_records(depths, poses, depth_scale):
             raise ValueError("%d frames but %d poses" % (len(depths), len(poses)))
         first = depths[0]
         for d in depths:
+            L.device_tensor(d, "depth")
             if d.shape != first.shape or d.dtype != first.dtype or d.stride() != first.stride():
                 return np.concatenate([np.frombuffer(bytes(make_frame(d, p, depth_scale)), L.frame_dtype())
                                        for d, p in zip(depths, poses)])

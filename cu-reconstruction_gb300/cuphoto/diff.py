@@ -58,11 +58,11 @@ class DiffConfig:
 
 
 def _ptr(t):
-    return C.c_void_p(t.data_ptr())
+    return C.c_void_p(L.device_tensor(t, "tensor").data_ptr())
 
 
 def _opt(t):
-    return None if t is None else C.c_void_p(t.data_ptr())
+    return None if t is None else _ptr(t)
 
 
 def checkpoint_shape(nframes, grid_zyx):

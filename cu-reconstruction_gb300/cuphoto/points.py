@@ -105,14 +105,15 @@ class PointCloud:
         if depth.numel() == 0:
             _log("cudaPointCloud::extract_points() -- depth width/height parameters are zero")
             return False
+        L.device_image(depth, "depth", (torch.float32, torch.uint16, torch.int16))
         H, W = int(depth.shape[0]), int(depth.shape[1])
         fmt = L.DEPTH_U16 if depth.dtype in (torch.uint16, torch.int16) else L.DEPTH_F32_M
-        if fmt == L.DEPTH_F32_M and depth.dtype != torch.float32:
-            raise TypeError("depth must be float32 metres or uint16")
-        if colors is not None:
-            self.has_rgb = True
         cptr, cpitch = None, 0
         if colors is not None:
+            L.device_image(colors, "colors", (torch.uint8,), channels=3)
+            if tuple(colors.shape[:2]) != (H, W):
+                raise ValueError("colors are %dx%d, depth %dx%d" % (colors.shape[1], colors.shape[0], W, H))
+            self.has_rgb = True
             cptr, cpitch = C.c_void_p(colors.data_ptr()), int(colors.stride(0) * colors.element_size())
         start = int(frame_idx) * W * H
         st = L.lib().gbt_points_extract(C.byref(_k9(self.camera_matrix)), C.c_void_p(depth.data_ptr()),
@@ -128,10 +129,14 @@ class PointCloud:
 
     def _project(self, color, depth, camera_pose, stream):
         torch = _torch()
+        L.device_image(depth, "depth", (torch.float32,))
         H, W = int(depth.shape[0]), int(depth.shape[1])
         scratch = torch.empty(H * W, dtype=torch.int64, device="cuda")
         cptr, cpitch = None, 0
         if color is not None:
+            L.device_image(color, "color", (torch.uint8,), channels=3)
+            if tuple(color.shape[:2]) != (H, W):
+                raise ValueError("color is %dx%d, depth %dx%d" % (color.shape[1], color.shape[0], W, H))
             cptr, cpitch = C.c_void_p(color.data_ptr()), int(color.stride(0) * color.element_size())
         n = self.num_pts
         st = L.lib().gbt_points_project(C.c_void_p(self.device_pts.data_ptr()) if n else None, n,

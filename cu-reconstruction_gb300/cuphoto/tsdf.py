@@ -113,18 +113,12 @@ def _log_error(msg):
 def make_frame(depth, pose, depth_scale=0.001):
     """A gbt_frame for a CUDA depth tensor (H, W) of float32 metres or uint16."""
     torch = _torch()
+    L.device_image(depth, "depth", (torch.float32, torch.uint16, torch.int16))
     f = L.Frame()
     f.depth = depth.data_ptr()
     f.height, f.width = int(depth.shape[0]), int(depth.shape[1])
     f.pitch_bytes = int(depth.stride(0) * depth.element_size())
-    if depth.dtype == torch.float32:
-        f.format = L.DEPTH_F32_M
-    elif depth.dtype in (torch.uint16, torch.int16):
-        f.format = L.DEPTH_U16
-    else:
-        raise TypeError("depth must be float32 metres or uint16, got %s" % depth.dtype)
-    if depth.stride(1) != 1:
-        raise ValueError("depth rows must be contiguous")
+    f.format = L.DEPTH_F32_M if depth.dtype == torch.float32 else L.DEPTH_U16
     f.depth_scale = float(depth_scale)
     for k in range(7):
         f.pose[k] = float(pose[k])

@@ -234,16 +234,22 @@ def test_volume_files_rejected_before_any_device_work(engine_lib, tmp_path):
     assert not out.value
 
 
-def test_bulk_frame_records_match_single_frames(engine_lib):
+def test_bulk_frame_records_match_single_frames(engine_lib, monkeypatch):
     """The batch API's numpy frame records are byte-identical to the ctypes
     gbt_frame of each frame, for a list of images and for one 3-D tensor
-    (CPU tensors: only their pointers and strides are read)."""
+    (CPU tensors, whose pointers and strides alone are read: the device check
+    is lifted here, where nothing is launched)."""
     torch = pytest.importorskip("torch")
     import numpy as np
     from cuphoto.batch import _frame_records
     from cuphoto.tsdf import make_frame
     L = engine_lib
     frames = torch.zeros((5, 48, 64), dtype=torch.int16)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        make_frame(frames[0], np.zeros(7), 0.001)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        _frame_records(frames, np.zeros((5, 7)), 0.001)
+    monkeypatch.setattr(L, "device_tensor", lambda t, name: t)
     poses = np.random.default_rng(0).normal(size=(5, 7))
     single = b"".join(bytes(make_frame(frames[k], poses[k], 0.001)) for k in range(5))
     assert _frame_records(frames, poses, 0.001).tobytes() == single
