@@ -58,13 +58,13 @@ __device__ __forceinline__ f2 f2_pack(float lo, float hi) {
 }
 __device__ __forceinline__ f2 f2_splat(float x) { return f2_pack(x, x); }
 __device__ __forceinline__ float f2_lo(f2 v) {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v.r));
+    float lo;
+    asm("mov.b64 {%0, _}, %1;" : "=f"(lo) : "l"(v.r));
     return lo;
 }
 __device__ __forceinline__ float f2_hi(f2 v) {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v.r));
+    float hi;
+    asm("mov.b64 {_, %0}, %1;" : "=f"(hi) : "l"(v.r));
     return hi;
 }
 __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
