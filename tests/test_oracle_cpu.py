@@ -99,6 +99,33 @@ def test_fastdiv_matches_integer_division():
             assert fastdiv_dev(n, f) == n // d, (n, d)
 
 
+def test_fused_uint16_conversion_is_the_rounded_product():
+    """The integrate kernels form a uint16 sample as fma(2^23 + raw, scale,
+    -2^23 * scale), 2^23 + raw being the float with the bits of 2^23 OR raw,
+    for scales whose biased exponent lies in 1..231.  Restated here with the
+    exact sum in float64 (a 24-bit by 24-bit product and a 40-bit result fit
+    its 53 bits) rounded once to float32, as the fused multiply-add rounds:
+    equal to float32(raw) * scale for every raw value, none of the products
+    subnormal, and 2^23 * scale exact."""
+    raw = np.arange(65536, dtype=np.uint32)
+    a = (raw | np.uint32(0x4B000000)).view(np.float32)
+    assert np.array_equal(a.astype(np.float64), raw + 8388608.0)
+    rng = np.random.default_rng(3)
+    scales = [np.float32(2.0 ** -126), np.nextafter(np.float32(2.0 ** 105), np.float32(0)), np.float32(0.001),
+              np.float32(1e-3 / 3), np.float32(0.0002), np.float32(1.0), np.float32(-0.001)]
+    scales += [np.float32(x) for x in 2.0 ** rng.uniform(-126, 105, 40)]
+    for sc in scales:
+        e = (int(np.float32(sc).view(np.uint32)) >> 23) & 0xFF
+        assert 1 <= e <= 231
+        bias = np.float32(-8388608.0) * sc
+        assert float(bias) == -8388608.0 * float(sc)              # exact
+        fused = (a.astype(np.float64) * float(sc) + float(bias)).astype(np.float32)
+        plain = raw.astype(np.float32) * sc
+        assert np.array_equal(fused.view(np.uint32)[1:], plain.view(np.uint32)[1:]), sc
+        assert fused[0] == 0 and plain[0] == 0                    # (signs of zero aside)
+        assert np.all(np.abs(plain[1:]) >= np.finfo(np.float32).tiny)
+
+
 def small_cfg(**kw):
     base = dict(voxel_grid_size=(16, 12, 8), physical_size=(0.8, 0.6, 0.4), global_offset=(-0.4, -0.3, 0.6),
                 focal_x=100.0, focal_y=100.0, cx=31.5, cy=23.5, camera_width=64, camera_height=48, max_weight=64)
