@@ -1,0 +1,26 @@
+"""bench.py's reference arm (the CPU port timed on the host cores): its JSON
+line keeps the benchmark contract (no GPU needed)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1",
+                        "--grid", "128"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    sys.path.insert(0, ROOT)
+    import bench
+    assert j["impl"] == "reference" and j["metric"] == bench.METRIC and j["unit"] == bench.UNIT
+    assert j["steps"] == 2 and j["warmup"] == 1 and j["n_gpus"] == 1 and j["higher_is_better"] is True
+    assert j["value"] > 0 and j["ms_per_step"] > 0
+    cb = j["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == j["value"] and cb["sample"]
+    assert j["e2e"] == {"value": j["value"], "unit": j["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert j["config"]["grid"] == 128
