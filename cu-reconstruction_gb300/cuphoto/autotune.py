@@ -3,7 +3,8 @@
 Each candidate integrates the same frames into the volume (which is reset
 before and after), timed with CUDA events on the launching stream; the
 fastest is kept.  Results are cached per (GPU, grid, image size, mode,
-arithmetic, build of the engine library) in a JSON file next to the library.
+arithmetic, build of the engine library, candidate sets) in a JSON file next
+to the library.
 """
 import json
 import os
@@ -39,7 +40,7 @@ def _load():
 def _store(d):
     try:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-        tmp = CACHE + ".tmp"
+        tmp = "%s.%d.tmp" % (CACHE, os.getpid())   # one per process: ranks may tune at once
         with open(tmp, "w") as f:
             json.dump(d, f, indent=1, sort_keys=True)
         os.replace(tmp, CACHE)
@@ -52,7 +53,7 @@ def tune_integrate(vol, depths, poses, depth_scale=0.001, bricks=BRICKS, frames=
     """Returns {"brick", "frames", "ctas", "ns_per_update", "table"} for this volume and frame size."""
     import torch
     h, w = int(depths[0].shape[0]), int(depths[0].shape[1])
-    key = _key(vol, w, h)
+    key = _key(vol, w, h) + "|pass|%s|%s|%s" % (tuple(bricks), tuple(frames), tuple(ctas))
     cache = _load() if use_cache else {}
     if key in cache:
         return cache[key]
@@ -101,7 +102,7 @@ def tune_batched(vol, depths, poses, batch, depth_scale=0.001, bricks=(0, 1, 2, 
     "table"}; "frames" is the window."""
     import torch
     h, w = int(depths[0].shape[0]), int(depths[0].shape[1])
-    key = _key(vol, w, h) + "|batched|%d" % len(depths)
+    key = _key(vol, w, h) + "|batched|%d|%s|%s|%s" % (len(depths), tuple(bricks), tuple(windows), tuple(ctas))
     cache = _load() if use_cache else {}
     if key in cache:
         return cache[key]

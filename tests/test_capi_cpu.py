@@ -261,3 +261,16 @@ def test_bulk_frame_records_match_single_frames(engine_lib, monkeypatch):
     assert mixed["pitch_bytes"].tolist() == [128, 320]
     with pytest.raises(ValueError):
         _frame_records(frames, poses[:4], 0.001)
+
+
+def test_autotune_cache_round_trip(engine_lib, tmp_path, monkeypatch):
+    """The tuner's JSON cache: stored through a per-process temporary file,
+    read back, and an unreadable cache counts as empty (tuning again)."""
+    from cuphoto import autotune as A
+    monkeypatch.setattr(A, "CACHE", str(tmp_path / "tune" / "autotune.json"))
+    assert A._load() == {}
+    A._store({"k": {"brick": 2, "frames": 64, "ctas": 0}})
+    assert A._load() == {"k": {"brick": 2, "frames": 64, "ctas": 0}}
+    assert sorted(p.name for p in (tmp_path / "tune").iterdir()) == ["autotune.json"]
+    (tmp_path / "tune" / "autotune.json").write_text("{not json")
+    assert A._load() == {}
