@@ -48,6 +48,8 @@ public:
     // frames: device depth images; poses: world-to-camera {qw,qx,qy,qz,tx,ty,tz}.
     // resume_from: a volume file (TSDFVolume::save) to continue instead of an
     // empty volume; save_to: where to write the volume after the frames.
+    // Throws CuPhotoException when the volume cannot be created or loaded, a
+    // pass of frames is refused, or the volume cannot be saved.
     void reconstruct_sequence(const std::vector<gbt_frame>& frames, i32 frames_per_pass = 16,
                               const std::string& resume_from = "", const std::string& save_to = "");
 

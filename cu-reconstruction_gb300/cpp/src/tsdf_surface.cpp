@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <string>
 
 #include "cuphoto/cp_exception.hpp"
 #include "cuphoto/marching_cubes.cuh"
@@ -126,7 +127,10 @@ void TSDFSurface::reconstruct_sequence(const std::vector<gbt_frame>& frames, i32
     if (frames_per_pass > GBT_MAX_FRAMES_PER_PASS) frames_per_pass = GBT_MAX_FRAMES_PER_PASS;
     for (size_t s = 0; s < frames.size(); s += (size_t)frames_per_pass) {
         const i32 n = (i32)((frames.size() - s) < (size_t)frames_per_pass ? frames.size() - s : (size_t)frames_per_pass);
-        if (!tsdf_volume->integrate_frames(frames.data() + s, n)) return;
+        // (integrate_frames has logged the engine's message)
+        if (!tsdf_volume->integrate_frames(frames.data() + s, n))
+            throw CuPhotoException("TSDFSurface::reconstruct_sequence: integrating frames " + std::to_string(s) +
+                                   ".." + std::to_string(s + (size_t)n - 1) + " failed");
     }
     cudaDeviceSynchronize();
     if (!save_to.empty() && !tsdf_volume->save(save_to))
