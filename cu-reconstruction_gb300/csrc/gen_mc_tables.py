@@ -18,8 +18,9 @@ This script stores it in a different, denser form:
   from the triangle list and checked here against the reference's own edge
   table (``marching_cubes_tables.cuh:18``).
 
-Run it from the repository root in a checkout where the reference is present:
-``python cu-reconstruction_gb300/csrc/gen_mc_tables.py /root/reference``.
+Run it from the repository root, naming the reference checkout (argument or
+``REFERENCE_ROOT``):
+``python cu-reconstruction_gb300/csrc/gen_mc_tables.py <reference checkout>``.
 """
 import os
 import re
@@ -108,7 +109,9 @@ def emit(packed, counts, masks, ends):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT")
+    if not ref_root:
+        sys.exit("usage: gen_mc_tables.py <reference checkout>  (or set REFERENCE_ROOT)")
     ends, edge_table, tri = load_reference_tables(ref_root)
     packed, counts, masks = pack(ends, edge_table, tri)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mc_tables.inc")

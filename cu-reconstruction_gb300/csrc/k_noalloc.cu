@@ -122,6 +122,7 @@ gbt_status gbt_extract_mesh_noalloc(gbt_volume* v, float* verts, int32_t* tris, 
     a.group_bits = reinterpret_cast<uint32_t*>(a.status + a.ntiles);
     a.tile_list = a.group_bits + nwords;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaGetLastError();  // a launch reports only its own failure, not one left pending by an earlier call
     // the previous call's ticket, flags, counts and tile words must not leak into this one
     e = cudaMemsetAsync(scratch, 0, 64 + nsuper * 16 + (size_t)a.ntiles * 8 + nwords * 4, st);
     if (e == cudaSuccess && a.ntiles > 0) {

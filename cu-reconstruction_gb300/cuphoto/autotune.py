@@ -37,13 +37,25 @@ def _load():
         return {}
 
 
-def _store(d):
+def _store(key, value):
+    """Adds one entry to the cache file.  The file is reloaded under an
+    exclusive lock and the entry merged in, so ranks that tune at once keep
+    each other's entries; each process writes through its own temporary file
+    and renames it over the cache (readers never see a torn file)."""
     try:
+        import fcntl
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-        tmp = "%s.%d.tmp" % (CACHE, os.getpid())   # one per process: ranks may tune at once
-        with open(tmp, "w") as f:
-            json.dump(d, f, indent=1, sort_keys=True)
-        os.replace(tmp, CACHE)
+        with open(CACHE + ".lock", "a") as lk:
+            fcntl.flock(lk, fcntl.LOCK_EX)
+            try:
+                d = _load()
+                d[key] = value
+                tmp = "%s.%d.tmp" % (CACHE, os.getpid())
+                with open(tmp, "w") as f:
+                    json.dump(d, f, indent=1, sort_keys=True)
+                os.replace(tmp, CACHE)
+            finally:
+                fcntl.flock(lk, fcntl.LOCK_UN)
     except OSError:
         pass
 
@@ -86,8 +98,7 @@ def tune_integrate(vol, depths, poses, depth_scale=0.001, bricks=BRICKS, frames=
     torch.cuda.synchronize()
     res = {"brick": best[0], "frames": best[1], "ctas": best[2], "ns_per_update": best[3], "table": table}
     if use_cache:
-        cache[key] = res
-        _store(cache)
+        _store(key, res)
     return res
 
 
@@ -135,6 +146,5 @@ def tune_batched(vol, depths, poses, batch, depth_scale=0.001, bricks=(0, 1, 2, 
     torch.cuda.synchronize()
     res = {"brick": best[0], "frames": best[1], "ctas": best[2], "ns_per_update": best[3], "table": table}
     if use_cache:
-        cache[key] = res
-        _store(cache)
+        _store(key, res)
     return res

@@ -273,7 +273,9 @@ gbt_status gbt_extract_mesh(gbt_volume* vol, float* verts, int32_t* tris, int64_
                             int64_t* n_tris, void* stream);
 
 /* Asynchronous form of gbt_extract_mesh: the count is written to the device
- * word *d_n_tris and nothing is synchronised; usable inside stream capture. */
+ * word *d_n_tris (the kernels' raw total, also if they set their error word)
+ * and nothing is synchronised; usable inside stream capture once the volume
+ * has been meshed before (its first mesh may allocate the tile scratch). */
 gbt_status gbt_extract_mesh_async(gbt_volume* vol, float* verts, int32_t* tris, int64_t cap_tris,
                                   int64_t index_base, int64_t* d_n_tris, void* stream);
 
@@ -307,9 +309,15 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* vol, float* verts, float* normal
  *
  * Output as gbt_extract_mesh_async: up to cap_tris triangles into verts/tris
  * and the count into the device word *d_n_tris.  Asynchronous on `stream`.
+ * One difference: if the kernels set their error word (none of the current
+ * kernels ever does), *d_n_tris receives -1 here, where the _async form
+ * copies the raw total.
  *
  * The first call on a device resolves the array's address (and may load the
  * library's device code), so make that first call before any stream capture.
+ * The address is kept per device for the life of the process: after
+ * cudaDeviceReset the module is loaded again, and this call must not be used
+ * in that process any more.
  * All calls share the one array and it keeps the previous call's contents:
  * each call clears it on `stream` first, and calls whose work overlaps on the
  * GPU (other streams, other host threads) race -- serialise them.

@@ -269,8 +269,35 @@ def test_autotune_cache_round_trip(engine_lib, tmp_path, monkeypatch):
     from cuphoto import autotune as A
     monkeypatch.setattr(A, "CACHE", str(tmp_path / "tune" / "autotune.json"))
     assert A._load() == {}
-    A._store({"k": {"brick": 2, "frames": 64, "ctas": 0}})
+    A._store("k", {"brick": 2, "frames": 64, "ctas": 0})
     assert A._load() == {"k": {"brick": 2, "frames": 64, "ctas": 0}}
-    assert sorted(p.name for p in (tmp_path / "tune").iterdir()) == ["autotune.json"]
+    A._store("k2", {"brick": 1, "frames": 32, "ctas": 16})
+    assert sorted(A._load()) == ["k", "k2"]
+    assert sorted(p.name for p in (tmp_path / "tune").iterdir()) == ["autotune.json", "autotune.json.lock"]
     (tmp_path / "tune" / "autotune.json").write_text("{not json")
     assert A._load() == {}
+
+
+def _store_keys(cache, rank, n):
+    from cuphoto import autotune as A
+    A.CACHE = cache
+    for i in range(n):
+        A._store("rank%d-%d" % (rank, i), {"brick": rank, "frames": i, "ctas": 0})
+
+
+def test_autotune_cache_keeps_every_process_entries(engine_lib, tmp_path):
+    """Processes that tune at once (ranks of one job) all keep their entries:
+    each store reloads the file under a lock and merges its key in."""
+    import multiprocessing as mp
+    cache = str(tmp_path / "autotune.json")
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_store_keys, args=(cache, r, 8)) for r in range(3)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    import json
+    with open(cache) as f:
+        d = json.load(f)
+    assert sorted(d) == sorted("rank%d-%d" % (r, i) for r in range(3) for i in range(8))

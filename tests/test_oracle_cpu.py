@@ -12,7 +12,14 @@ from cuphoto import synthetic as S
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLES = os.path.join(HERE, "..", "cu-reconstruction_gb300", "csrc", "mc_tables.inc")
-REF_TABLES = "/root/reference/modules/include/cuda/marching_cubes_tables.cuh"
+def _reference_root():
+    # the reference checkout the oracle recipe builds from (REFERENCE_ROOT)
+    import oracle.build
+    return oracle.build.REF_ROOT
+
+
+REF_ROOT = _reference_root()
+REF_TABLES = os.path.join(REF_ROOT, "modules", "include", "cuda", "marching_cubes_tables.cuh")
 
 # reference corner numbering (marching_cubes.cu:118-127)
 DX = [0, 1, 1, 0, 0, 1, 1, 0]
@@ -61,7 +68,7 @@ def test_tables_match_reference_file():
         "gen", os.path.join(HERE, "..", "cu-reconstruction_gb300", "csrc", "gen_mc_tables.py"))
     gen = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(gen)
-    ends, edge_table, tri = gen.load_reference_tables("/root/reference")
+    ends, edge_table, tri = gen.load_reference_tables(REF_ROOT)
     e2, count, mask, packed = load_tables()
     assert ends == e2
     assert mask == edge_table
