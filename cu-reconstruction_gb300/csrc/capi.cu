@@ -33,6 +33,33 @@ gbt_status cuda_fail(cudaError_t e, const char* what) {
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
+// Host-side failure injection (gbt_debug_inject): allocations to let through
+// before failing, and how many to fail after that.
+std::atomic<int64_t> g_inject_skip{0};
+std::atomic<int64_t> g_inject_fail{0};
+
+// true if this allocation is one that gbt_debug_inject asked to fail
+bool injected_alloc_failure() {
+    if (g_inject_fail.load() <= 0) return false;
+    if (g_inject_skip.fetch_sub(1) > 0) return false;
+    g_inject_skip.store(0);
+    return g_inject_fail.fetch_sub(1) > 0;
+}
+
+// Every device, managed and pinned allocation of the engine goes through
+// these, so that failure injection reaches each of them.
+cudaError_t dev_alloc(void** p, size_t bytes, bool managed = false) {
+    if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
+    return managed ? cudaMallocManaged(p, bytes, cudaMemAttachGlobal) : cudaMalloc(p, bytes);
+}
+
+cudaError_t pinned_alloc(void** p, size_t bytes) {
+    if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
+    return cudaMallocHost(p, bytes);
+}
+
+__global__ void injected_launch_kernel() {}
+
 // SMs of the device current at the first call (the thread-safe
 // initialisation of a function-local static; every device here is alike)
 int device_sms() {
@@ -172,6 +199,28 @@ const char* gbt_last_error(void) { return g_last_error.c_str(); }
 
 const char* gbt_version(void) { return "gbt-tsdf 0.1 sm_103a"; }
 
+gbt_status gbt_debug_inject(int32_t what, int64_t skip, int64_t count) {
+    switch (what) {
+        case GBT_INJECT_NONE:
+            g_inject_fail.store(0);
+            g_inject_skip.store(0);
+            return GBT_OK;
+        case GBT_INJECT_ALLOC:
+            if (skip < 0 || count < 0) return fail(GBT_ERR_INVALID_ARG, "gbt_debug_inject: negative skip or count");
+            g_inject_fail.store(0);
+            g_inject_skip.store(skip);
+            g_inject_fail.store(count);
+            return GBT_OK;
+        case GBT_INJECT_LAUNCH_ERROR:
+            // a block of zero threads: the runtime refuses the launch on the
+            // host (invalid configuration); nothing reaches the GPU
+            injected_launch_kernel<<<1, 0>>>();
+            return GBT_OK;
+        default:
+            return fail(GBT_ERR_INVALID_ARG, "gbt_debug_inject: unknown kind %d", what);
+    }
+}
+
 gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume** out) {
     gbt::TraceRange trace_("gbt_volume_create");
     if (!cfg || !out) return fail(GBT_ERR_INVALID_ARG, "cfg or out is NULL");
@@ -235,11 +284,11 @@ gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume
     const size_t bytes = (size_t)nvox * sizeof(float);
     cudaError_t e;
     if (v->managed) {
-        e = cudaMallocManaged(&d.D, bytes, cudaMemAttachGlobal);
-        if (e == cudaSuccess) e = cudaMallocManaged(&d.W, bytes, cudaMemAttachGlobal);
+        e = dev_alloc(reinterpret_cast<void**>(&d.D), bytes, true);
+        if (e == cudaSuccess) e = dev_alloc(reinterpret_cast<void**>(&d.W), bytes, true);
     } else {
-        e = cudaMalloc(&d.D, bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&d.W, bytes);
+        e = dev_alloc(reinterpret_cast<void**>(&d.D), bytes);
+        if (e == cudaSuccess) e = dev_alloc(reinterpret_cast<void**>(&d.W), bytes);
     }
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -418,7 +467,7 @@ gbt_status gbt_volume_transformation_voxels(gbt_volume* v, void* stream, void** 
     if (!v || !out) return fail(GBT_ERR_INVALID_ARG, "volume or out is NULL");
     if (!v->tvox) {
         const size_t bytes = (size_t)v->nvox * 28;
-        cudaError_t e = v->managed ? cudaMallocManaged(&v->tvox, bytes, cudaMemAttachGlobal) : cudaMalloc(&v->tvox, bytes);
+        cudaError_t e = dev_alloc(&v->tvox, bytes, v->managed);
         if (e != cudaSuccess) {
             cudaGetLastError();
             v->tvox = nullptr;
@@ -536,7 +585,7 @@ gbt_status mc_prepare(gbt_volume* v, float* verts, int32_t* tris, int64_t cap, i
         if (v->mc_scratch) cudaFree(v->mc_scratch);
         v->mc_scratch = nullptr;
         v->mc_scratch_bytes = 0;
-        cudaError_t e = cudaMalloc(&v->mc_scratch, need);
+        cudaError_t e = dev_alloc(&v->mc_scratch, need);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return fail(GBT_ERR_ALLOC, "allocating %zu bytes of mesh scratch: %s", need, cudaGetErrorString(e));
@@ -653,8 +702,8 @@ gbt_status gbt_batch_create(int32_t max_scenes, int32_t max_frames, gbt_batch** 
     b->max_scenes = max_scenes;
     b->max_frames = max_frames;
     b->bytes = batch_bytes(max_scenes, max_frames);
-    cudaError_t e = cudaMallocHost(&b->host, b->bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&b->dev, b->bytes);
+    cudaError_t e = pinned_alloc(&b->host, b->bytes);
+    if (e == cudaSuccess) e = dev_alloc(&b->dev, b->bytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -944,7 +993,7 @@ gbt_status gbt_extract_mesh_indexed(gbt_volume* v, float* verts, float* normals,
         if (v->weld_scratch) cudaFree(v->weld_scratch);
         v->weld_scratch = nullptr;
         v->weld_scratch_bytes = 0;
-        cudaError_t e = cudaMalloc(&v->weld_scratch, need);
+        cudaError_t e = dev_alloc(&v->weld_scratch, need);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return fail(GBT_ERR_ALLOC, "allocating %zu bytes of vertex-sharing scratch: %s", need, cudaGetErrorString(e));

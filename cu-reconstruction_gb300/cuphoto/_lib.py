@@ -30,6 +30,9 @@ DEPTH_U16 = 1
 MEMORY_DEVICE = 0
 MEMORY_MANAGED = 1
 MAX_FRAMES_PER_PASS = 32
+INJECT_NONE = 0
+INJECT_ALLOC = 1
+INJECT_LAUNCH_ERROR = 2
 
 
 class VolumeCfg(C.Structure):
@@ -152,6 +155,7 @@ SIGNATURES = [
     ("gbt_image_filter_if", C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                       C.c_void_p]),
     ("gbt_last_error", C.c_char_p, []),
+    ("gbt_debug_inject", C.c_int, [C.c_int32, C.c_int64, C.c_int64]),
     ("gbt_version", C.c_char_p, []),
 ]
 

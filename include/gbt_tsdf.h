@@ -396,6 +396,25 @@ gbt_status gbt_image_filter_if(float* image, int64_t pitch_bytes, int32_t width,
 /* Message for the last failure on the calling thread ("" if none). */
 const char* gbt_last_error(void);
 
+/* Host-side failure injection, for tests of the error paths.  No counterpart
+ * in the reference, whose constructor swallows exactly these failures
+ * (tsdf_volume.cu:203-209: a failed cudaMallocManaged is logged and the
+ * volume is used anyway).
+ *   GBT_INJECT_ALLOC: after `skip` more device, managed or pinned
+ *     allocations made by the engine succeed, the next `count` fail as
+ *     cudaErrorMemoryAllocation would (nothing is allocated for them).
+ *   GBT_INJECT_LAUNCH_ERROR: leaves a launch error pending in the engine's
+ *     CUDA runtime, as a caller's failed launch would: a kernel launched with
+ *     a block of zero threads, which the runtime refuses on the host.
+ *   GBT_INJECT_NONE: cancels pending allocation failures.
+ * Nothing here touches the GPU or its memory. */
+enum {
+    GBT_INJECT_NONE = 0,
+    GBT_INJECT_ALLOC = 1,
+    GBT_INJECT_LAUNCH_ERROR = 2
+};
+gbt_status gbt_debug_inject(int32_t what, int64_t skip, int64_t count);
+
 /* Engine version string. */
 const char* gbt_version(void);
 

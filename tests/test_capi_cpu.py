@@ -301,3 +301,28 @@ def test_autotune_cache_keeps_every_process_entries(engine_lib, tmp_path):
     with open(cache) as f:
         d = json.load(f)
     assert sorted(d) == sorted("rank%d-%d" % (r, i) for r in range(3) for i in range(8))
+
+
+def test_injected_allocation_failure_before_any_device_work(engine_lib):
+    """gbt_debug_inject: the volume's first allocation fails on the host side;
+    the call reports GBT_ERR_ALLOC with the size in gbt_last_error and leaves
+    no handle (the reference's constructor logs such a failure and carries
+    on, tsdf_volume.cu:203-209)."""
+    L = engine_lib
+    lib = L.lib()
+    assert lib.gbt_debug_inject(L.INJECT_ALLOC, 0, 1) == L.GBT_OK
+    c = _cfg(L)
+    out = C.c_void_p(12345)
+    st = lib.gbt_volume_create(C.byref(c), None, C.byref(out))
+    assert st == L.GBT_ERR_ALLOC
+    assert out.value is None
+    msg = lib.gbt_last_error().decode()
+    assert "allocating 4096 bytes for the volume" in msg and "out of memory" in msg
+    # the same for the batch tables' pinned staging copy
+    assert lib.gbt_debug_inject(L.INJECT_ALLOC, 0, 1) == L.GBT_OK
+    b = C.c_void_p(1)
+    assert lib.gbt_batch_create(4, 16, C.byref(b)) == L.GBT_ERR_ALLOC
+    assert b.value is None and "batch tables" in lib.gbt_last_error().decode()
+    assert lib.gbt_debug_inject(L.INJECT_NONE, 0, 0) == L.GBT_OK
+    assert lib.gbt_debug_inject(L.INJECT_ALLOC, -1, 1) == L.GBT_ERR_INVALID_ARG
+    assert lib.gbt_debug_inject(7, 0, 0) == L.GBT_ERR_INVALID_ARG

@@ -78,3 +78,47 @@ def test_noalloc_rejects_volumes_beyond_its_scratch(gpu):
     assert st == L.GBT_ERR_INVALID_ARG
     msg = lib.gbt_last_error().decode()
     assert "static scratch" in msg and "201060352" in msg
+
+
+def test_noalloc_mesh_recorded_in_global_mode_graph_capture(gpu):
+    """The use the entry point exists for: recording mesh extraction into a
+    CUDA graph captured in the global mode, where any cudaMalloc would fail
+    the capture.  One call first (it resolves the scratch address), then the
+    capture; two replays give gbt_extract_mesh's triangles and count."""
+    grid = (64, 72, 80)
+    tc = TSDFVolumeConfig(voxel_grid_size=grid, physical_size=(0.64, 0.72, 0.8), mode="fixed", arith="ieee",
+                          max_weight=8)
+    vol = TSDFVolume(tc)
+    vol.voxel_distances_data().copy_(gpu.from_numpy(smooth_field(grid[::-1], 5)).cuda())
+    vol.voxel_weights_data().fill_(1.0)
+    gpu.cuda.synchronize()
+    V0, T0 = extract_mesh_device(vol)
+    V0, T0 = V0.cpu().numpy(), T0.cpu().numpy()
+    assert len(V0) > 500
+    lib = L.lib()
+    cap = len(V0) + 8
+    verts = gpu.zeros((cap, 3, 3), dtype=gpu.float32, device="cuda")
+    tris = gpu.zeros((cap, 3), dtype=gpu.int32, device="cuda")
+    count = gpu.zeros(1, dtype=gpu.int64, device="cuda")
+
+    def call():
+        st = lib.gbt_extract_mesh_noalloc(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
+                                          cap, 0, C.c_void_p(count.data_ptr()),
+                                          C.c_void_p(gpu.cuda.current_stream().cuda_stream))
+        assert st == L.GBT_OK, lib.gbt_last_error().decode()
+
+    call()
+    gpu.cuda.synchronize()
+    g = gpu.cuda.CUDAGraph()
+    with gpu.cuda.graph(g, capture_error_mode="global"):
+        call()
+    for _ in range(2):
+        verts.zero_()
+        tris.zero_()
+        count.fill_(-2)
+        g.replay()
+        gpu.cuda.synchronize()
+        n = int(count.item())
+        assert n == len(V0)
+        assert np.array_equal(verts[:n].cpu().numpy().view(np.uint32), V0.view(np.uint32))
+        assert np.array_equal(tris[:n].cpu().numpy(), T0)
