@@ -272,17 +272,11 @@ def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=3):
     return out
 
 
-def differentiable_c3(torch, reps=20):
-    """Forward + adjoint of the differentiable integrate at 128^3, 16 frames
-    320x240 (FP32): CUDA-event times of the plain forward, the forward that
-    writes the adjoint's checkpoints and the adjoint, their ratio, and the
-    directional-derivative error of the FP64 and FP32 adjoints against FP64
-    central differences on the GPU (steps h and h/2, Richardson-extrapolated;
-    the plain step-h difference also given) along unit directions over all
-    poses (h = 1e-4 and 1e-5) and over all valid depth pixels (h = 1e-4)."""
+def _diff_tools(torch, case):
+    """Forward, adjoint and FD-check closures of the differentiable integrate
+    for one case (a dict of synthetic.diff_case_*)."""
     from cuphoto import diff as DF
     from cuphoto import synthetic as S
-    case = S.diff_case_frontal(128, 16)
     cfg = DF.DiffConfig(case["grid"], tuple(float(v) for v in case["vs"]), tuple(float(v) for v in case["off"]),
                         *case["K"], truncation=case["trunc"], max_weight=case["max_weight"],
                         max_depth=case["max_depth"], min_z=case["min_z"])
@@ -311,53 +305,11 @@ def differentiable_c3(torch, reps=20):
         gpose = torch.zeros((F, 12), dtype=torch.float64, device="cuda")
         return (gD, gW, D0, W0, gdep, gpose), lambda: DF.backward_raw(cfg, gD, gW, D0, W0, ck, *a, gdep, gpose)
 
-    # timing, FP32
-    R32, t32, dep32 = case["R"], case["t"], case["depth"]
-    D, W, ck, _, a = forward(R32, t32, dep32, torch.float32, ckpt=True)
-    bufs, run_adj = adjoint(D, W, ck, a, torch.ones(shape, dtype=torch.bool, device="cuda"), torch.float32)
-    Dp = torch.empty_like(D)
-    Wp = torch.empty_like(W)
-
-    def fwd_plain():
-        Dp.fill_(case["trunc"])
-        Wp.zero_()
-        DF.forward_raw(cfg, Dp, Wp, *a)
-
-    def fwd_ckpt():
-        Dp.fill_(case["trunc"])
-        Wp.zero_()
-        DF.forward_raw(cfg, Dp, Wp, *a, ck)
-
-    def fill_only():
-        Dp.fill_(case["trunc"])
-        Wp.zero_()
-
-    def adj():
-        bufs[4].zero_()
-        bufs[5].zero_()
-        run_adj()
-
-    def timed(fn):
-        for _ in range(3):
-            fn()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            fn()
-        e1.record()
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps
-
-    t_fill = timed(fill_only)
-    t_plain = timed(fwd_plain) - t_fill
-    t_ckpt = timed(fwd_ckpt) - t_fill
-    t_adj = timed(adj) - timed(lambda: (bufs[4].zero_(), bufs[5].zero_()))
-    nvf = int(np.prod(shape)) * F
-
-    # FD check, FP64 on the GPU
     def fd_check(which, h):
+        """FP64 and FP32 adjoints against FP64 central differences (steps h
+        and h/2, Richardson-extrapolated) of L = sum W (D - sdf_gt)^2 along a
+        unit direction over all poses or over every valid depth pixel, on the
+        voxels whose discrete decisions are the same at every perturbed input."""
         rng = np.random.default_rng(3)
         dphi = rng.normal(size=(F, 3))
         dtr = rng.normal(size=(F, 3))
@@ -406,6 +358,70 @@ def differentiable_c3(torch, reps=20):
                 "rel_err_fp64_vs_plain_fd": abs(an64 - d1) / abs(d1),
                 "voxels_compared": float(mask.float().mean().item())}
 
+    return cfg, forward, adjoint, fd_check
+
+
+def differentiable_c3(torch, reps=20):
+    """Forward + adjoint of the differentiable integrate on the 128^3,
+    16-frame 320x240 configuration (seeded plane + 6 spheres, circle cameras,
+    uint16 depth with noise and dropped pixels; FP32): CUDA-event times of
+    the plain forward, the forward that writes the adjoint's checkpoints and
+    the adjoint, their ratio; the directional-derivative errors of the FP64
+    and FP32 adjoints against FP64 central differences on the GPU along all
+    poses (steps 1e-4 and 1e-5) and all valid depth pixels (1e-4); the same
+    pose check at steps 1e-4 and 1e-5 on the ground plane alone with exact
+    depth (no depth edges in view); FP32 against FP64 gradients."""
+    from cuphoto import diff as DF
+    from cuphoto import synthetic as S
+    case = S.diff_case_c3(128, 16)
+    cfg, forward, adjoint, fd_check = _diff_tools(torch, case)
+    shape = case["grid"][::-1]
+    F = len(case["R"])
+
+    # timing, FP32
+    D, W, ck, _, a = forward(case["R"], case["t"], case["depth"], torch.float32, ckpt=True)
+    bufs, run_adj = adjoint(D, W, ck, a, torch.ones(shape, dtype=torch.bool, device="cuda"), torch.float32)
+    Dp = torch.empty_like(D)
+    Wp = torch.empty_like(W)
+
+    def fwd_plain():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+        DF.forward_raw(cfg, Dp, Wp, *a)
+
+    def fwd_ckpt():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+        DF.forward_raw(cfg, Dp, Wp, *a, ck)
+
+    def fill_only():
+        Dp.fill_(case["trunc"])
+        Wp.zero_()
+
+    def adj():
+        bufs[4].zero_()
+        bufs[5].zero_()
+        run_adj()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_fill = timed(fill_only)
+    t_plain = timed(fwd_plain) - t_fill
+    t_ckpt = timed(fwd_ckpt) - t_fill
+    t_adj = timed(adj) - timed(lambda: (bufs[4].zero_(), bufs[5].zero_()))
+    nvf = int(np.prod(shape)) * F
+
     def fp32_vs_fp64():
         D64, W64, ck64, s64, a64 = forward(case["R"], case["t"], case["depth"], torch.float64, ckpt=True, sig=True)
         D32, W32, ck32, s32, a32 = forward(case["R"], case["t"], case["depth"], torch.float32, ckpt=True, sig=True)
@@ -418,12 +434,17 @@ def differentiable_c3(torch, reps=20):
         return {"voxels_same_decisions": float(m.float().mean().item()), "grad_depth_rel_l2": rel(b32[4], b64[4]),
                 "grad_pose_rel_l2": rel(b32[5], b64[5])}
 
-    return {"config": "128^3 voxels, 16 frames 320x240 float32 depth, frontal plane+spheres scene, "
-                      "L = sum W (D - sdf_gt)^2",
+    smooth = S.diff_case_c3(128, 16, smooth=True)
+    _, _, _, fd_smooth = _diff_tools(torch, smooth)
+    return {"config": "128^3 voxels of 2 cm, 16 frames 320x240 (fx=fy=262.5, cx=159.5, cy=119.5) on the 1.5 m "
+                      "circle, seeded plane + 6 spheres, uint16 mm depth with 1 mm noise and 2% dropped pixels, "
+                      "truncation 4 voxels, L = sum W (D - sdf_gt)^2",
             "forward_ms": t_plain, "forward_with_checkpoints_ms": t_ckpt, "adjoint_ms": t_adj,
             "fwd_plus_adjoint_over_fwd": (t_ckpt + t_adj) / t_plain,
             "forward_voxel_updates_per_s": nvf / (t_plain * 1e-3),
             "fd_pose": [fd_check("pose", 1e-4), fd_check("pose", 1e-5)], "fd_depth": fd_check("depth", 1e-4),
+            "fd_pose_plane_scene": {"scene": "ground plane alone, exact depth (no depth edges in view)",
+                                    "checks": [fd_smooth("pose", 1e-4), fd_smooth("pose", 1e-5)]},
             "fp32_vs_fp64": fp32_vs_fp64()}
 
 

@@ -1031,6 +1031,191 @@ __global__ void __launch_bounds__(kMcThreads) mc_count_kernel(const __grid_const
     }
 }
 
+// Row-walking count with four voxel columns per lane, for grids whose rows
+// and layers start on 16-byte boundaries (x extent and layer stride
+// multiples of 4).  A warp takes a segment of 128 voxel columns (128 cubes:
+// lane l holds columns x0 + 4l .. x0 + 4l + 3 and their cubes; the x + 1
+// column of its last cube is lane l + 1's first, or for lane 31 the first
+// column of the next segment, which it loads alone) and walks
+// kMcRows4PerTask rows along y.  Per row a lane loads two 16-byte vectors of
+// distances (layers z and z + 1; two more of weights in the fixed mode) and
+// packs their signs into four nibbles; the nibble of a cube's x corners is
+// the previous row's two bits and this row's two, and (x, x + 1) nibble
+// pairs index the triangle-count table.  Rows where no lane's cubes change
+// sign skip the table.
+constexpr uint32_t kMcSeg4Cubes = 128;
+constexpr uint32_t kMcRows4PerTask = 32;
+
+template <int MODE>
+__device__ __forceinline__ uint32_t mc_sign_bits4(const float4& p, const float4& q) {
+    // bit 4j: column j below zero in layer z; bit 4j + 1: in layer z + 1
+    return (uint32_t)(p.x < 0.f) | (uint32_t)(q.x < 0.f) << 1 | (uint32_t)(p.y < 0.f) << 4 |
+           (uint32_t)(q.y < 0.f) << 5 | (uint32_t)(p.z < 0.f) << 8 | (uint32_t)(q.z < 0.f) << 9 |
+           (uint32_t)(p.w < 0.f) << 12 | (uint32_t)(q.w < 0.f) << 13;
+}
+__device__ __forceinline__ uint32_t mc_weight_bits4(const float4& p, const float4& q) {
+    // bit j: column j observed (weight > 0) in both layers
+    return (uint32_t)(p.x > 0.f && q.x > 0.f) | (uint32_t)(p.y > 0.f && q.y > 0.f) << 1 |
+           (uint32_t)(p.z > 0.f && q.z > 0.f) << 2 | (uint32_t)(p.w > 0.f && q.w > 0.f) << 3;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kMcThreads) mc_count4_kernel(const __grid_constant__ McArgs a) {
+    __shared__ unsigned char s_cnt[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) s_cnt[k] = GBT_MC_TRI_COUNT[mc_type_of_nibbles(k & 15, k >> 4)];
+    __syncthreads();
+    constexpr int kShift = kMcTileShift[MODE];
+    static_assert(mc_tile_cubes(MODE) >= 2 * kMcSeg4Cubes, "a row segment straddles at most one tile boundary");
+    constexpr uint32_t kBatch = MODE == kFixed ? 2 : 4;   // rows whose loads are in flight together
+    const int lane = threadIdx.x & 31;
+    const uint32_t gx = (uint32_t)a.gx, gy = (uint32_t)a.gy;
+    const uint32_t cx_n = gx - 1, cy_n = gy - 1, cz_n = (uint32_t)a.gz - 1;
+    const uint32_t nseg = (cx_n + kMcSeg4Cubes - 1) / kMcSeg4Cubes;
+    const uint32_t nchunk = (cy_n + kMcRows4PerTask - 1) / kMcRows4PerTask;
+    const uint64_t ntasks = (uint64_t)cz_n * nchunk * nseg;
+    const uint32_t layer = (MODE == kCompat) ? gx + gy : gx * gy;   // marching_cubes.cu:211
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t task = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntasks; task += nwarps) {
+        const uint32_t seg = (uint32_t)(task % nseg);
+        const uint64_t rest = task / nseg;
+        const uint32_t chunk = (uint32_t)(rest % nchunk);
+        const uint32_t cz = (uint32_t)(rest / nchunk);
+        const uint32_t x0 = seg * kMcSeg4Cubes;
+        const uint32_t xb = x0 + 4u * (uint32_t)lane;            // this lane's first column
+        const uint32_t xl = xb < gx ? xb : gx - 4;                // (loads stay in the grid)
+        const uint32_t xe = x0 + kMcSeg4Cubes;                     // lane 31's extra column
+        const bool extra = lane == 31 && xe < gx;
+        // the lane's cubes inside the grid: bit j for cube xb + j
+        const uint32_t cm = xb >= cx_n ? 0u : (cx_n - xb >= 4 ? 15u : (1u << (cx_n - xb)) - 1u);
+        const uint32_t y0 = chunk * kMcRows4PerTask;
+        const uint32_t y1 = min(y0 + kMcRows4PerTask, cy_n);
+        const uint32_t r0 = cz * layer + y0 * gx;                  // voxel (0, y0, z); + layer: z + 1
+        const float4* dp = reinterpret_cast<const float4*>(a.D + r0 + xl);
+        const float4* dq = reinterpret_cast<const float4*>(a.D + r0 + layer + xl);
+        const float4* wp = reinterpret_cast<const float4*>(a.W + r0 + xl);
+        const float4* wq = reinterpret_cast<const float4*>(a.W + r0 + layer + xl);
+        const float* ep = a.D + r0 + (extra ? xe : 0u);
+        const float* eq = ep + layer;
+        const float* vp = a.W + r0 + (extra ? xe : 0u);
+        const float* vq = vp + layer;
+        const uint32_t row4 = gx >> 2;   // a grid row in 16-byte vectors
+        // row y0: the lower nibble halves
+        uint32_t lo = mc_sign_bits4<MODE>(__ldg(dp), __ldg(dq));
+        uint32_t lo_e = extra ? ((uint32_t)(__ldg(ep) < 0.f) | (uint32_t)(__ldg(eq) < 0.f) << 1) : 0u;
+        uint32_t vlo = 15u, vlo_e = 1u;
+        if (MODE == kFixed) {
+            vlo = mc_weight_bits4(__ldg(wp), __ldg(wq));
+            vlo_e = extra ? (uint32_t)(__ldg(vp) > 0.f && __ldg(vq) > 0.f) : 0u;
+        }
+        uint32_t c_row = (cz * cy_n + y0) * cx_n;    // linear index of cube (0, y, z)
+        uint32_t cur = (c_row + x0) >> kShift;       // tile of the warp's first cube
+        unsigned acc0 = 0, acc1 = 0;                 // this lane's triangles in tiles cur and cur + 1
+        auto flush = [&]() {
+            const unsigned n0 = __reduce_add_sync(0xffffffffu, acc0);
+            const unsigned n1 = __reduce_add_sync(0xffffffffu, acc1);
+            if (lane == 0) {
+                if (n0) mc_add_tile(a, cur, n0);
+                if (n1) mc_add_tile(a, cur + 1, n1);
+            }
+            acc0 = 0;
+            acc1 = 0;
+        };
+        auto row = [&](float4 p, float4 q, float pe, float qe, float4 wpv, float4 wqv, float wpe, float wqe) {
+            if (((c_row + x0) >> kShift) != cur) {   // the same for the whole warp
+                flush();
+                cur = (c_row + x0) >> kShift;
+            }
+            const uint32_t hi = mc_sign_bits4<MODE>(p, q);
+            const uint32_t hi_e = (uint32_t)(pe < 0.f) | (uint32_t)(qe < 0.f) << 1;
+            const uint32_t nib = lo | hi << 2;                 // nibble j: the x corners of cube j
+            const uint32_t nib_e = lo_e | hi_e << 2;
+            // every lane takes part in the shuffles
+            const uint32_t nx = __shfl_down_sync(0xffffffffu, nib & 15u, 1);
+            const uint32_t n20 = nib | (lane == 31 ? nib_e : nx) << 16;
+            uint32_t ok = cm;
+            uint32_t vhi = 15u, vhi_e = 1u;
+            if (MODE == kFixed) {
+                vhi = mc_weight_bits4(wpv, wqv);
+                vhi_e = (uint32_t)(wpe > 0.f && wqe > 0.f);
+                const uint32_t vv = vlo & vhi, vv_e = vlo_e & vhi_e;
+                const uint32_t vn = __shfl_down_sync(0xffffffffu, vv & 1u, 1);
+                const uint32_t v5 = vv | (lane == 31 ? vv_e : vn) << 4;
+                ok &= v5 & (v5 >> 1);
+            }
+            const bool mixed = ok != 0u && n20 != 0u && n20 != 0xFFFFFu;
+            if (__any_sync(0xffffffffu, mixed)) {
+                const uint32_t c0 = c_row + xb;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const unsigned n = ((ok >> j) & 1u) ? s_cnt[(n20 >> (4 * j)) & 0xFFu] : 0u;
+                    const uint32_t c = c0 + (uint32_t)j;
+                    if ((c >> kShift) == cur) acc0 += n; else acc1 += n;
+                    // the cube's group of 32 (linear order) has triangles: the
+                    // emit kernel visits only such groups
+                    if (n) atomicOr(a.group_bits + (c >> 10), 1u << ((c >> 5) & 31u));
+                }
+            }
+            lo = hi;
+            lo_e = hi_e;
+            vlo = vhi;
+            vlo_e = vhi_e;
+            c_row += cx_n;
+        };
+        uint32_t y = y0;
+        for (; y + kBatch <= y1; y += kBatch) {
+            float4 p[kBatch], q[kBatch], u[kBatch], v[kBatch];
+            float pe[kBatch], qe[kBatch], ue[kBatch], ve[kBatch];
+#pragma unroll
+            for (uint32_t j = 0; j < kBatch; ++j) {
+                const size_t o = (size_t)(j + 1) * row4;
+                const size_t oe = (size_t)(j + 1) * gx;
+                p[j] = __ldg(dp + o);
+                q[j] = __ldg(dq + o);
+                pe[j] = extra ? __ldg(ep + oe) : 0.f;
+                qe[j] = extra ? __ldg(eq + oe) : 0.f;
+                if (MODE == kFixed) {
+                    u[j] = __ldg(wp + o);
+                    v[j] = __ldg(wq + o);
+                    ue[j] = extra ? __ldg(vp + oe) : 0.f;
+                    ve[j] = extra ? __ldg(vq + oe) : 0.f;
+                }
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < kBatch; ++j) {
+                if (MODE == kFixed)
+                    row(p[j], q[j], pe[j], qe[j], u[j], v[j], ue[j], ve[j]);
+                else
+                    row(p[j], q[j], pe[j], qe[j], p[j], q[j], 0.f, 0.f);
+            }
+            dp += (size_t)kBatch * row4;
+            dq += (size_t)kBatch * row4;
+            wp += (size_t)kBatch * row4;
+            wq += (size_t)kBatch * row4;
+            ep += (size_t)kBatch * gx;
+            eq += (size_t)kBatch * gx;
+            vp += (size_t)kBatch * gx;
+            vq += (size_t)kBatch * gx;
+        }
+        for (; y < y1; ++y) {   // the rows after the last full batch
+            dp += row4;
+            dq += row4;
+            wp += row4;
+            wq += row4;
+            ep += gx;
+            eq += gx;
+            vp += gx;
+            vq += gx;
+            const float4 p = __ldg(dp), q = __ldg(dq);
+            const float pe = extra ? __ldg(ep) : 0.f, qe = extra ? __ldg(eq) : 0.f;
+            if (MODE == kFixed)
+                row(p, q, pe, qe, __ldg(wp), __ldg(wq), extra ? __ldg(vp) : 0.f, extra ? __ldg(vq) : 0.f);
+            else
+                row(p, q, pe, qe, p, q, 0.f, 0.f);
+        }
+        flush();
+    }
+}
+
 constexpr int kMcScanThreads = 1 << kMcSuperShift;   // one thread per tile of a superblock
 
 // Exclusive offsets of the tiles (in place), the list of tiles with
@@ -1095,166 +1280,201 @@ __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_co
     }
 }
 
-// Emission: a CTA takes the next listed tile, classifies its cubes, scans
-// the triangle counts (warp scans, then warp 0 over the partial sums) and
-// writes every cube's triangles from the tile's offset.
+// Emission.  Warps take the listed tiles in turn (warp w of the grid: list
+// entries w, w + warps, ...; no CTA waits on another warp).  For each group
+// of 32 consecutive cubes that the count kernel marked, in cube order, a
+// warp classifies the group again (lane l: cube l; its x corners loaded, its
+// x + 1 corners the next lane's, or loaded by the lane when the next cube
+// starts a new row or lies in the next group), scans the triangle counts and
+// then emits the group's triangles 32 at a time, one triangle per lane: the
+// lane finds its cube and the triangle's place in the cube's case from a
+// per-warp slot table, takes the cube's type and corner values from the
+// owning lane by shuffles, and stages the vertices in shared memory, so that
+// the warp writes consecutive triangles with coalesced stores.
+constexpr int kMcEmitMaxPerGroup = 32 * 5;   // triangles of a group of 32 cubes, at most
+
+template <int MODE>
+__device__ __forceinline__ void mc_vertex(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int64_t b0, int64_t b1,
+                                          float sa, float sb, int ca, int cb, float* out) {
+    float pa[3], pb[3];
+    if (MODE == kCompat) {
+        if (sa > 0 && sb < 0) {  // marching_cubes.cu:34-41
+            const int tc = ca; ca = cb; cb = tc;
+            const float ts = sa; sa = sb; sb = ts;
+        }
+        // corner positions come from the voxel at the same linear index
+        const int64_t ia = corner_index<MODE>(a, b0, b1, ca);
+        const int64_t ib = corner_index<MODE>(a, b0, b1, cb);
+        const uint32_t ra = fastdiv((uint32_t)ia, a.div_gx), rb = fastdiv((uint32_t)ib, a.div_gx);
+        const uint32_t za = fastdiv(ra, a.div_gy), zb = fastdiv(rb, a.div_gy);
+        pa[0] = centre((int)((uint32_t)ia - ra * (uint32_t)a.gx), a.vs[0], a.off[0]);
+        pa[1] = centre((int)(ra - za * (uint32_t)a.gy), a.vs[1], a.off[1]);
+        pa[2] = centre((int)za, a.vs[2], a.off[2]);
+        pb[0] = centre((int)((uint32_t)ib - rb * (uint32_t)a.gx), a.vs[0], a.off[0]);
+        pb[1] = centre((int)(rb - zb * (uint32_t)a.gy), a.vs[1], a.off[1]);
+        pb[2] = centre((int)zb, a.vs[2], a.off[2]);
+        const float r = mc_ratio(sa, sb);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) out[q] = mc_lerp(pa[q], pb[q], r);
+    } else {
+#if !defined(GBT_REF_ARITH)
+        // lower endpoint first, so the cubes sharing the edge agree
+        if (corner_dx(ca) + corner_dy(ca) + corner_dz(ca) > corner_dx(cb) + corner_dy(cb) + corner_dz(cb)) {
+            const int tc = ca; ca = cb; cb = tc;
+            const float ts = sa; sa = sb; sb = ts;
+        }
+        pa[0] = centre((int)cx + corner_dx(ca), a.vs[0], a.off[0]);
+        pa[1] = centre((int)cy + corner_dy(ca), a.vs[1], a.off[1]);
+        pa[2] = centre((int)cz + corner_dz(ca), a.vs[2], a.off[2]);
+        pb[0] = centre((int)cx + corner_dx(cb), a.vs[0], a.off[0]);
+        pb[1] = centre((int)cy + corner_dy(cb), a.vs[1], a.off[1]);
+        pb[2] = centre((int)cz + corner_dz(cb), a.vs[2], a.off[2]);
+        const float r = __fdiv_rn(sa, __fsub_rn(sa, sb));
+#pragma unroll
+        for (int q = 0; q < 3; ++q) out[q] = __fmaf_rn(r, __fsub_rn(pb[q], pa[q]), pa[q]);
+#endif
+    }
+}
+
+// Shared-vertex index of the fixed-mode edge (ca, cb) of cube (cx, cy, cz).
+__device__ __forceinline__ int32_t mc_vertex_index(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int ca,
+                                                   int cb) {
+    if (corner_dx(ca) + corner_dy(ca) + corner_dz(ca) > corner_dx(cb) + corner_dy(cb) + corner_dz(cb)) {
+        const int tc = ca; ca = cb; cb = tc;
+    }
+    const int64_t id = weld_edge_id(a, cx, cy, cz, ca, cb);
+    const uint32_t word = a.edge_bits[id >> 5];
+    const uint32_t below = word & ((1u << (id & 31)) - 1u);
+    return (int32_t)(a.index_base + a.edge_word_offset[id >> 5] + __popc(below));
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_constant__ McArgs a) {
+    constexpr int kWarps = kMcThreads / 32;
     __shared__ unsigned char s_count[256];
     __shared__ unsigned long long s_tri[256];
     __shared__ unsigned char s_ends[12];
     __shared__ unsigned char s_type[256];
-    constexpr int kWarps = kMcThreads / 32;
-    constexpr int CPT = mc_cubes_per_thread(MODE);
-    constexpr int kTile = kMcThreads * CPT;
-    constexpr int kParts = CPT * kWarps;   // partial sums per tile, in linear cube order
-    static_assert(kParts % 32 == 0 && kParts <= 32 * 4, "warp 0 scans the partial sums, up to 4 per lane");
-    constexpr int kPerLane = kParts / 32;
-    __shared__ int s_wsum[kParts];
-    __shared__ unsigned int s_job;
-
-    const int tid = threadIdx.x;
+    __shared__ unsigned char s_slot[kWarps][kMcEmitMaxPerGroup];   // owner lane | triangle of its case << 5
+    __shared__ float s_out[kWarps][32 * 9];                         // a batch of 32 triangles
+    __shared__ float s_val[kWarps][8][32];                          // corner values of each lane's cube
     mc_load_tables(s_count, s_tri, s_ends, s_type);
-    const int lane = tid & 31, warp = tid >> 5;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned njobs = *a.nonempty;
-
-    for (;;) {
-        __syncthreads();
-        if (tid == 0) s_job = atomicAdd(a.ticket, 1u);
-        __syncthreads();
-        const unsigned job = s_job;
-        if (job >= njobs) return;
+    constexpr uint32_t kWords = (uint32_t)mc_tile_cubes(MODE) / 1024u;   // group words per tile
+    const uint32_t nwords = (a.ncubes + 1023u) / 1024u;
+    const bool indexed = MODE == kFixed && a.edge_bits != nullptr;
+    const unsigned gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
+    unsigned char* slot = s_slot[warp];
+    float* sout = s_out[warp];
+    float (*sval)[32] = s_val[warp];
+    for (unsigned job = gw; job < njobs; job += nw) {
         const uint32_t tile = a.tile_list[job];
-        const long long tile_prefix = (long long)a.status[tile];
-        const uint32_t c0 = tile * (uint32_t)kTile;
-
-        int type[CPT];
-        int incl[CPT];
-        // the warp's CPT consecutive groups of 32 cubes; only the groups the
-        // count kernel marked have triangles and are classified again
-        {
-            const uint64_t wbase = (uint64_t)c0 + (uint64_t)warp * (32 * CPT);
+        long long out0 = (long long)a.status[tile];   // this tile's first triangle
+#pragma unroll 1
+        for (uint32_t w = 0; w < kWords; ++w) {
+            const uint32_t word = tile * kWords + w;
+            uint32_t bits = word < nwords ? a.group_bits[word] : 0u;   // the same for the whole warp
+            while (bits) {
+                const uint32_t g = (uint32_t)__ffs(bits) - 1u;
+                bits &= bits - 1u;
+                const uint64_t cube = (uint64_t)(word * 32u + g) * 32u + (uint64_t)lane;
+                const bool in = cube < a.ncubes;
+                const uint32_t c = in ? (uint32_t)cube : a.ncubes - 1u;
+                // classification: x corners (0, 3, 4, 7) loaded, x + 1 corners (1, 2, 5, 6)
+                // from the next lane or loaded
+                uint32_t idx[4];
+                const bool own = cube_xcorners<MODE>(a, c, idx) || lane == 31;
+                float X[4], N[4], WX[4];
 #pragma unroll
-            for (int i = 0; i < CPT; ++i) {
-                const uint64_t g = (wbase >> 5) + i;
-                type[i] = 0;
-                // (the last tile may run past the last cube and its group word)
-                if (g * 32 < a.ncubes && ((a.group_bits[g >> 5] >> (g & 31)) & 1u)) {   // the same for the whole warp
-                    int t1[1];
-                    mc_warp_types<MODE, 1>(a, wbase + 32 * i, lane, t1, s_type);
-                    type[i] = t1[0];
+                for (int k = 0; k < 4; ++k) {
+                    X[k] = __ldg(a.D + idx[k]);
+                    if (MODE == kFixed) WX[k] = __ldg(a.W + idx[k]);
                 }
-            }
-        }
+                bool okn = true;
 #pragma unroll
-        for (int i = 0; i < CPT; ++i) {
-            int n = s_count[type[i]];
-            // inclusive warp scan
+                for (int k = 0; k < 4; ++k) N[k] = __shfl_down_sync(0xffffffffu, X[k], 1);
+                bool okx = true;
+                if (MODE == kFixed) okx = WX[0] > 0.f && WX[1] > 0.f && WX[2] > 0.f && WX[3] > 0.f;
+                if (MODE == kFixed) okn = __shfl_down_sync(0xffffffffu, okx ? 1 : 0, 1) != 0;
+                if (own) {
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, n, o);
-                if (lane >= o) n += y;
-            }
-            incl[i] = n;
-            if (lane == 31) s_wsum[warp * CPT + i] = n;   // group warp * CPT + i of the tile
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // exclusive scan of the kParts partial sums, kPerLane consecutive ones per lane
-            int v[kPerLane];
-            int local = 0;
-#pragma unroll
-            for (int q = 0; q < kPerLane; ++q) {
-                v[q] = s_wsum[lane * kPerLane + q];
-                local += v[q];
-            }
-            int x = local;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            int run = x - local;
-#pragma unroll
-            for (int q = 0; q < kPerLane; ++q) {
-                s_wsum[lane * kPerLane + q] = run;
-                run += v[q];
-            }
-        }
-        __syncthreads();
-
-#pragma unroll
-        for (int i = 0; i < CPT; ++i) {
-            const int t = type[i];
-            const int n = s_count[t];
-            if (!n) continue;
-            long long out = tile_prefix + s_wsum[warp * CPT + i] + incl[i] - n;
-            if (out >= a.cap) continue;
-            const uint32_t c = c0 + (warp * CPT + i) * 32 + lane;
-            const uint32_t row = fastdiv(c, a.div_cx);
-            const uint32_t cx = c - row * (uint32_t)(a.gx - 1);
-            const uint32_t cz = fastdiv(row, a.div_cy);
-            const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
-            int64_t b0, b1;
-            cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
-            float val[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) val[k] = __ldg(a.D + corner_index<MODE>(a, b0, b1, k));
-            const unsigned long long edges = s_tri[t];
-            for (int tr = 0; tr < n; ++tr, ++out) {
-                if (out >= a.cap) break;
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const int e = (int)((edges >> (4 * (3 * tr + j))) & 15ull);
-                    int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
-                    float pa[3], pb[3];
-                    float sa = val[ca], sb = val[cb];
-                    if (MODE == kCompat) {
-                        if (sa > 0 && sb < 0) {  // marching_cubes.cu:34-41
-                            const int tc = ca; ca = cb; cb = tc;
-                            const float ts = sa; sa = sb; sb = ts;
-                        }
-                        // corner positions come from the voxel at the same linear index
-                        const int64_t ia = corner_index<MODE>(a, b0, b1, ca);
-                        const int64_t ib = corner_index<MODE>(a, b0, b1, cb);
-                        const uint32_t ra = fastdiv((uint32_t)ia, a.div_gx), rb = fastdiv((uint32_t)ib, a.div_gx);
-                        const uint32_t za = fastdiv(ra, a.div_gy), zb = fastdiv(rb, a.div_gy);
-                        pa[0] = centre((int)((uint32_t)ia - ra * (uint32_t)a.gx), a.vs[0], a.off[0]);
-                        pa[1] = centre((int)(ra - za * (uint32_t)a.gy), a.vs[1], a.off[1]);
-                        pa[2] = centre((int)za, a.vs[2], a.off[2]);
-                        pb[0] = centre((int)((uint32_t)ib - rb * (uint32_t)a.gx), a.vs[0], a.off[0]);
-                        pb[1] = centre((int)(rb - zb * (uint32_t)a.gy), a.vs[1], a.off[1]);
-                        pb[2] = centre((int)zb, a.vs[2], a.off[2]);
-                        const float r = mc_ratio(sa, sb);
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) a.verts[9 * out + 3 * j + q] = mc_lerp(pa[q], pb[q], r);
-                    } else {
-#if !defined(GBT_REF_ARITH)
-                        // lower endpoint first, so the cubes sharing the edge agree
-                        if (corner_dx(ca) + corner_dy(ca) + corner_dz(ca) > corner_dx(cb) + corner_dy(cb) + corner_dz(cb)) {
-                            const int tc = ca; ca = cb; cb = tc;
-                            const float ts = sa; sa = sb; sb = ts;
-                        }
-                        if (a.edge_bits) {   // shared vertices: the index of this edge's vertex
-                            const int64_t id = weld_edge_id(a, cx, cy, cz, ca, cb);
-                            const uint32_t word = a.edge_bits[id >> 5];
-                            const uint32_t below = word & ((1u << (id & 31)) - 1u);
-                            a.tris[3 * out + j] = (int32_t)(a.index_base + a.edge_word_offset[id >> 5] + __popc(below));
-                            continue;
-                        }
-                        pa[0] = centre((int)cx + corner_dx(ca), a.vs[0], a.off[0]);
-                        pa[1] = centre((int)cy + corner_dy(ca), a.vs[1], a.off[1]);
-                        pa[2] = centre((int)cz + corner_dz(ca), a.vs[2], a.off[2]);
-                        pb[0] = centre((int)cx + corner_dx(cb), a.vs[0], a.off[0]);
-                        pb[1] = centre((int)cy + corner_dy(cb), a.vs[1], a.off[1]);
-                        pb[2] = centre((int)cz + corner_dz(cb), a.vs[2], a.off[2]);
-                        const float r = __fdiv_rn(sa, __fsub_rn(sa, sb));
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) a.verts[9 * out + 3 * j + q] = __fmaf_rn(r, __fsub_rn(pb[q], pa[q]), pa[q]);
-#endif
+                    for (int k = 0; k < 4; ++k) {
+                        N[k] = __ldg(a.D + idx[k] + 1);
+                        if (MODE == kFixed) WX[k] = __ldg(a.W + idx[k] + 1);
                     }
-                    a.tris[3 * out + j] = (int32_t)(a.index_base + 3 * out + j);
+                    if (MODE == kFixed) okn = WX[0] > 0.f && WX[1] > 0.f && WX[2] > 0.f && WX[3] > 0.f;
                 }
+                int sx = 0, sn = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    sx |= (X[k] < 0.f) << k;
+                    sn |= (N[k] < 0.f) << k;
+                }
+                int type = s_type[sx | sn << 4];
+                if (!in || (MODE == kFixed && !(okx && okn))) type = 0;
+                const int n = s_count[type];
+                int incl = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                for (int k = 0; k < n; ++k) slot[incl - n + k] = (unsigned char)(lane | k << 5);
+                __syncwarp();
+                // the cube's eight corners in the reference's numbering
+                const float val[8] = {X[0], N[0], N[1], X[1], X[2], N[2], N[3], X[3]};
+                for (int base = 0; base < total; base += 32) {
+                    const int qi = base + lane;
+                    const bool act = qi < total;
+                    const int sl = act ? slot[qi] : 0;
+                    const int o = sl & 31, tr = sl >> 5;
+                    // every lane takes part in the shuffles
+                    const int t = __shfl_sync(0xffffffffu, type, o);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) sval[k][lane] = __shfl_sync(0xffffffffu, val[k], o);
+                    __syncwarp();
+                    const uint32_t cc = (uint32_t)((uint64_t)(word * 32u + g) * 32u) + (uint32_t)o;
+                    if (act) {
+                        const uint32_t row = fastdiv(cc, a.div_cx);
+                        const uint32_t cx = cc - row * (uint32_t)(a.gx - 1);
+                        const uint32_t cz = fastdiv(row, a.div_cy);
+                        const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+                        int64_t b0, b1;
+                        cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+                        const unsigned long long edges = s_tri[t];
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) {
+                            const int e = (int)((edges >> (4 * (3 * tr + j))) & 15ull);
+                            const int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
+                            if (indexed) {
+#if !defined(GBT_REF_ARITH)
+                                const long long out = out0 + qi;
+                                if (out < a.cap) a.tris[3 * out + j] = mc_vertex_index(a, cx, cy, cz, ca, cb);
+#endif
+                            } else {
+                                mc_vertex<MODE>(a, cx, cy, cz, b0, b1, sval[ca][lane], sval[cb][lane], ca, cb,
+                                                sout + 9 * lane + 3 * j);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    if (!indexed) {
+                        // consecutive triangles out0 + base ... : 9 floats and 3 indices each
+                        const int nt = min(32, total - base);
+                        const long long first = out0 + base;
+                        const long long fit = a.cap - first;          // triangles of the batch that fit
+                        const int nw9 = 9 * (int)(fit < nt ? (fit > 0 ? fit : 0) : nt);
+                        for (int f = lane; f < nw9; f += 32) a.verts[9 * first + f] = sout[f];
+                        for (int f = lane; f < nw9 / 3; f += 32)
+                            a.tris[3 * first + f] = (int32_t)(a.index_base + 3 * first + f);
+                    }
+                    __syncwarp();
+                }
+                out0 += total;
+                __syncwarp();   // the slot table is rewritten by the next group
             }
         }
     }
@@ -1541,10 +1761,10 @@ int resident_ctas_mode(int kind, int brick) {
     }
 }
 
-// The three marching-cubes launches; the scratch words (ticket, total, list
-// length, tile words) are zero when the first starts.
+// The three marching-cubes launches; the scratch words (total, list length,
+// tile words, group bits) are zero when the first starts.
 struct McGrid {
-    int sms, per_count, per_emit;
+    int sms, per_count, per_count4, per_emit;
 };
 
 // SMs and resident CTAs of the count and emit kernels (thread-safe
@@ -1552,37 +1772,55 @@ struct McGrid {
 template <int MODE>
 const McGrid& mc_grid() {
     static const McGrid g = [] {
-        McGrid r{1, 1, 1};
+        McGrid r{1, 1, 1, 1};
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r.per_count, mc_count_kernel<MODE>, kMcThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r.per_count4, mc_count4_kernel<MODE>, kMcThreads, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r.per_emit, mc_emit_kernel<MODE>, kMcThreads, 0);
         cudaGetLastError();
         if (r.sms < 1) r.sms = 1;
         if (r.per_count < 1) r.per_count = 1;
+        if (r.per_count4 < 1) r.per_count4 = 1;
         if (r.per_emit < 1) r.per_emit = 1;
         return r;
     }();
     return g;
 }
 
+// The four-column count kernel needs every row and layer of the distances
+// (and weights) to start on a 16-byte boundary.
+template <int MODE>
+bool mc_rows_of_4(const McArgs& a) {
+    const long long layer = MODE == kCompat ? (long long)a.gx + a.gy : (long long)a.gx * a.gy;
+    return a.gx >= 4 && a.gx % 4 == 0 && layer % 4 == 0 && (reinterpret_cast<uintptr_t>(a.D) & 15u) == 0 &&
+           (MODE == kCompat || (reinterpret_cast<uintptr_t>(a.W) & 15u) == 0);
+}
+
 template <int MODE>
 cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
     const McGrid& mg = mc_grid<MODE>();
-    const int sms = mg.sms, per_count = mg.per_count, per_emit = mg.per_emit;
-    // one warp per task (a segment of a cube layer, kMcRowsPerTask rows)
-    const long long nseg = (a.gx - 1 + (long long)kMcSegCubes - 1) / kMcSegCubes;
-    const long long nchunk = (a.gy - 1 + (long long)kMcRowsPerTask - 1) / kMcRowsPerTask;
+    const bool four = mc_rows_of_4<MODE>(a);
+    // one warp per task (a segment of a cube layer, a run of rows)
+    const long long seg = four ? kMcSeg4Cubes : kMcSegCubes;
+    const long long rows = four ? kMcRows4PerTask : kMcRowsPerTask;
+    const long long nseg = (a.gx - 1 + seg - 1) / seg;
+    const long long nchunk = (a.gy - 1 + rows - 1) / rows;
     const long long ntasks = (long long)(a.gz - 1) * nchunk * nseg;
-    long long grid = (long long)sms * per_count;
+    long long grid = (long long)mg.sms * (four ? mg.per_count4 : mg.per_count);
     const long long need = (ntasks + kMcThreads / 32 - 1) / (kMcThreads / 32);
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
-    mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
+    if (four)
+        mc_count4_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
+    else
+        mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
     mc_scan_kernel<<<(unsigned)((a.ntiles + kMcScanThreads - 1) / kMcScanThreads), kMcScanThreads, 0, s>>>(a);
-    grid = (long long)sms * per_emit;
-    if (grid > (long long)a.ntiles) grid = a.ntiles;
+    grid = (long long)mg.sms * mg.per_emit;
+    const long long tiles_per_cta = kMcThreads / 32;   // a warp per listed tile at least
+    if (grid > ((long long)a.ntiles + tiles_per_cta - 1) / tiles_per_cta)
+        grid = ((long long)a.ntiles + tiles_per_cta - 1) / tiles_per_cta;
     if (grid < 1) grid = 1;
     mc_emit_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
     return cudaGetLastError();

@@ -297,6 +297,37 @@ def diff_case_circle(n=128, frames=16, camera=None, scene_id=5, n_spheres=12):
                 height=cam.height, depth=depth, R=R, t=t, scene=scene)
 
 
+def diff_case_c3(n=128, frames=16, scene_id=3, smooth=False):
+    """The differentiable-integrate configuration (128^3, 16 frames 320x240):
+    the seeded plane + 6 spheres scene seen from `frames` cameras on the
+    1.5 m circle (fx = fy = 262.5, cx = 159.5, cy = 119.5), uint16 millimetre
+    depth with N(0, 1 mm) noise and 2 % dropped pixels, converted to metres
+    as the engine converts it (float32(raw) * float32(0.001)); an n^3 grid
+    over the 2.56 m cube centred on the scene, truncation 4 voxels; the
+    analytic truncated SDF of the scene as the loss target.
+
+    smooth=True gives the same cameras and grid over the ground plane alone,
+    with exact depth (no noise, no dropped pixels): a depth image without
+    edges inside the grid's view."""
+    cam = Camera.half()
+    scene = make_scene(scene_id, n_spheres=0 if smooth else 6)
+    poses = circle_poses(frames)
+    if smooth:
+        depth = np.stack([render_depth_m(scene, p, cam) for p in poses])
+        depth = np.where(np.isfinite(depth) & (depth < 8.0), depth, 0.0)
+    else:
+        depth = np.stack([u16_to_metres(render_depth_u16(scene, p, cam, frame_seed=100 * scene_id + k))
+                          for k, p in enumerate(poses)]).astype(np.float64)
+    vs = np.full(3, 2.56 / n, np.float32)
+    off = np.full(3, -1.28, np.float32)
+    trunc = float(np.float32(4 * vs[0]))
+    R = np.stack([matrix_from_quat(p[:4]) for p in poses])
+    t = np.stack([p[4:] for p in poses])
+    return dict(grid=(n, n, n), vs=vs, off=off, K=(cam.fx, cam.fy, cam.cx, cam.cy), trunc=trunc, max_weight=128.0,
+                max_depth=8.0, min_z=0.05, width=cam.width, height=cam.height, depth=depth, R=R, t=t,
+                gt=sdf_gt(scene, (n, n, n), vs, off, trunc), scene=scene)
+
+
 def make_sequence(n_frames, scene_id=0, camera=None, n_spheres=6, trajectory="circle", **kw):
     camera = camera or Camera()
     if trajectory == "frontal":

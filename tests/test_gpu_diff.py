@@ -49,10 +49,13 @@ def gpu_backward(torch, case, gD, gW, state, args, want_start=False):
     return out
 
 
-def c3_case():
-    """The 128^3, 16-frame, 320x240 configuration (float64 inputs for the
-    check, the analytic truncated SDF of the scene as the target)."""
-    return S.diff_case_frontal(128, 16)
+def c3_case(smooth=False):
+    """The 128^3, 16-frame, 320x240 configuration: seeded plane + spheres
+    scene, circle cameras, uint16 depth with noise and dropped pixels (float64
+    copies of its metres for the check), the analytic truncated SDF of the
+    scene as the target.  smooth=True: the ground plane alone with exact
+    depth, so no depth edge lies in the grid's view."""
+    return S.diff_case_c3(128, 16, smooth=smooth)
 
 
 def _oracle_cfg(oracle, case, dtype):
@@ -134,20 +137,27 @@ def c3_fd_check(torch, case, dphi, dtr, ddep, h=1e-4):
     return (4 * d2 - d1) / 3, an64, mask
 
 
-@pytest.mark.parametrize("which,h", [("pose", 1e-5), ("depth", 1e-4)])
-def test_c3_adjoint_against_fp64_central_differences(gpu, which, h):
+@pytest.mark.parametrize("smooth,which,h,tol", [
+    (False, "pose", 1e-4, 1e-4),
+    (False, "depth", 1e-4, 1e-5),
+    (False, "pose", 1e-5, 1e-6),
+    (True, "pose", 1e-5, 1e-5),
+    (True, "depth", 1e-4, 1e-5),
+])
+def test_c3_adjoint_against_fp64_central_differences(gpu, smooth, which, h, tol):
     """128^3 grid, 16 frames 320x240: the directional derivative along a random
     unit direction (all 16 poses, or every valid depth pixel) from FP64
     central differences on the GPU (steps h and h/2, Richardson-
     extrapolated) against the FP64 adjoint, on the voxels whose discrete
-    decisions are the same at every perturbed input: error bound 1e-5
-    relative (1e-4 is the target).
+    decisions are the same at every perturbed input.
 
-    Along the poses the step is 1e-5: bilinear depth across depth edges
-    gives the loss large higher derivatives there, and at step 1e-4 the
-    difference itself is off by ~1e-3 (its agreement with the adjoint goes
-    1.3e-3, 2.7e-5, 1.3e-6, 7e-9 at steps 1e-4, 3e-5, 1e-5, 3e-6 in FP64)."""
-    case = c3_case()
+    The configured scene meets the 1e-4 target at the configured step 1e-4
+    (measured 2.9e-6 along the poses, 6.9e-7 along the depths) and agrees to
+    5e-9 at step 1e-5.  The ground plane alone, seen at grazing angles, is
+    the harder case for the difference: its depth is a rational function of
+    the pixel row with a pole at the horizon, and at step 1e-4 the
+    difference is off by ~1e-4 (measured 9.6e-5); it is checked at step 1e-5."""
+    case = c3_case(smooth)
     dphi, dtr, ddep = diffcase.perturbation(case, seed=3)
     if which == "pose":
         ddep = ddep * 0
@@ -158,7 +168,7 @@ def test_c3_adjoint_against_fp64_central_differences(gpu, which, h):
     fd, an64, mask = c3_fd_check(gpu, case, dphi, dtr, ddep, h)
     assert mask.float().mean().item() > 0.5
     assert fd != 0.0
-    assert abs(an64 - fd) <= 1e-5 * abs(fd), (an64, fd)
+    assert abs(an64 - fd) <= tol * abs(fd), (an64, fd, abs(an64 - fd) / abs(fd))
 
 
 def test_c3_fp32_adjoint_against_fp64(gpu):
