@@ -206,7 +206,7 @@ def reference_cuda(args, cam, scene, poses, torch, nframes=8):
             "frames_timed": len(ms), "what": "TSDFVolume::integrate of the reference, one launch + sync per frame"}
 
 
-def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=3):
+def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=10):
     """The same frames in the fixed mode (camera-space SDF, a real surface;
     the compat field of a camera circling the scene has no zero crossing, so
     the compat mesh is empty as it is for the reference), then meshes of
@@ -237,27 +237,58 @@ def fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas, reps=3):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    def mesh_timer(vol):
+    peak, peak_kind = peaks()
+
+    def mesh_timer(vol, mode):
+        """The mesh as the timed step runs it: gbt_extract_mesh_async captured
+        in a CUDA graph, replayed `reps` times between CUDA events after three
+        warm-up replays; the distances (and weights) are 1 GiB, above L2."""
         n = C.c_int64()
-        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-        L.check(lib.gbt_extract_mesh(vol.handle, None, None, 0, 0, C.byref(n), st))
+        L.check(lib.gbt_extract_mesh(vol.handle, None, None, 0, 0, C.byref(n),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream)))
         cap = max(n.value, 1)
         verts = torch.empty((cap, 3, 3), dtype=torch.float32, device="cuda")
         tris = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
         count = torch.zeros(1, dtype=torch.int64, device="cuda")
+        stream = torch.cuda.Stream()
 
         def run():
             L.check(lib.gbt_extract_mesh_async(vol.handle, C.c_void_p(verts.data_ptr()), C.c_void_p(tris.data_ptr()),
-                                               cap, 0, C.c_void_p(count.data_ptr()), st))
-        ms = timed(run)
-        return {"ms": ms, "triangles": int(n.value), "triangles_per_s": n.value / (ms * 1e-3)}
+                                               cap, 0, C.c_void_p(count.data_ptr()),
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        with torch.cuda.stream(stream):
+            run()
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                run()
+            for _ in range(3):
+                g.replay()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                g.replay()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        assert int(count.item()) == n.value
+        # algorithmic bytes: distances read once (and weights in the fixed
+        # mode), 36 B of vertices + 12 B of indices per triangle, the count
+        alg = (8.0 if mode == "fixed" else 4.0) * nvox + 48.0 * n.value + 8
+        gbs = alg / (ms * 1e-3) / 1e9
+        return {"ms": ms, "triangles": int(n.value), "triangles_per_s": n.value / (ms * 1e-3),
+                "roofline": {"bound": "hbm", "algorithmic_bytes": alg, "achieved": gbs, "peak": peak,
+                             "unit": "GB/s", "frac": gbs / peak, "peak_kind": peak_kind},
+                "timing": "graph replay x %d, CUDA events" % reps}
 
     t_int = timed(integ)
     out = {"integrate_voxel_updates_per_s": nvox * len(depths) / (t_int * 1e-3), "integrate_ms": t_int,
-           "mesh_fixed": mesh_timer(vf)}
+           "mesh_fixed": mesh_timer(vf, "fixed")}
     vc = TSDFVolume(volume_cfg(args, cam, "compat"))
     vc.voxel_distances_data().copy_(vf.voxel_distances_data())
-    out["mesh_compat_same_field"] = mesh_timer(vc)
+    out["mesh_compat_same_field"] = mesh_timer(vc, "compat")
     import oracle
     if oracle.RefHarness.available():
         r = oracle.RefHarness(volume_cfg(args, cam, "compat"))
@@ -901,6 +932,20 @@ def multiscene(args, torch, rank, world, local):
     }
 
 
+def multiscene_summary(args, torch, local):
+    """The multi-scene configuration (16 seeded scenes, 64^3..384^3, 10..120
+    frames, one batched launch per window, autotuned, graph-captured) run
+    inside the default line: its aggregate, integrate-only and end-to-end
+    rates and the per-scene rates (3 timed steps after 1 warm-up)."""
+    import copy
+    a2 = copy.copy(args)
+    a2.steps, a2.warmup, a2.config, a2.mode, a2.split_scenes = 3, 1, "", "compat", False
+    r = multiscene(a2, torch, 0, 1, local)
+    return {"value": r["value"], "unit": r["unit"], "ms_per_step": r["ms_per_step"], "steps": 3, "warmup": 1,
+            "config": r["config"], "breakdown_ms": r["breakdown_ms"], "integrate_only": r["integrate_only"],
+            "e2e": r["e2e"], "per_scene": r["per_scene"], "clocks": r["clocks"]}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1021,6 +1066,13 @@ def main():
         path, tune = ("batched", t_batched) if ms_batched < ms_single else ("single", t_single)
     K, brick, ctas = tune["frames"], tune["brick"], tune["ctas"]
     n_passes = (nf + K - 1) // K
+    # the fastest tuned candidate inside the configuration's 8-32 frames per launch
+    in_cfg = None
+    if not args.config:
+        cands = [(ns, "batched", b_, k_, c_) for (b_, k_, c_, ns) in t_batched["table"] if k_ <= 32]
+        cands += [(ns, "single", b_, k_, c_) for (b_, k_, c_, ns) in t_single["table"] if k_ <= 32]
+        if cands:
+            in_cfg = min(cands)[1:]
 
     def integrate_all():
         if path == "batched":
@@ -1154,6 +1206,39 @@ def main():
             d2h = Vh.numel() * 4 + Th.numel() * 4 + 8
     e2e_value = shard.whole_job_rate(nvox * nf, float(np.mean(e2e_ms)) * 1e-3)
 
+    # the configuration's own launch shape (8-32 frames per launch): reset +
+    # integrate captured as one graph and timed the same way as the step
+    integrate_in_config = None
+    if in_cfg is not None and world == 1:
+        p_, b_, k_, c_ = in_cfg
+
+        def integ_cfg():
+            vol.reset()
+            if p_ == "batched":
+                batch.integrate([vol], [depths], [poses], brick=b_, ctas_per_sm=c_, frames_per_launch=k_)
+            else:
+                vol.integrate_sequence(depths, poses, frames_per_pass=k_, brick=b_, ctas_per_sm=c_)
+        with torch.cuda.stream(stream):
+            integ_cfg()
+            torch.cuda.synchronize()
+            g_cfg = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g_cfg, stream=stream):
+                integ_cfg()
+            for _ in range(args.warmup):
+                g_cfg.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                g_cfg.replay()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms_cfg = e0.elapsed_time(e1) / args.steps
+        integrate_in_config = {"value": nvox * nf / (ms_cfg * 1e-3), "unit": UNIT, "ms_per_step": ms_cfg,
+                               "path": p_, "frames_per_launch": k_, "brick": b_, "ctas_per_sm": c_,
+                               "what": "reset + integrate of the 300 frames, fastest tuned candidate with at "
+                                       "most 32 frames per launch, graph replay x %d" % args.steps}
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -1163,6 +1248,7 @@ def main():
         extras["reference_cuda"] = reference_cuda(args, cam, scene, poses, torch)
         extras["fixed_mode_mesh"] = fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas)
         extras["differentiable"] = differentiable_c3(torch)
+        extras["multiscene"] = multiscene_summary(args, torch, local)
         cpu = cpu_baseline(args, cam, scene, poses)
     else:
         cpu = None
@@ -1194,6 +1280,11 @@ def main():
         "wall_s_timed": t_wall,
         "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": candidates},
     }
+    if integrate_in_config is not None:
+        out["integrate_in_config"] = integrate_in_config
+    if "fixed_mode_mesh" in extras:
+        # marching cubes of a field with a surface (the fixed-mode field of the same frames)
+        out["mesh_with_surface"] = extras["fixed_mode_mesh"]["mesh_fixed"]
     if cpu is not None:
         out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     out.update(extras)

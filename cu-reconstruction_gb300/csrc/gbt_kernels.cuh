@@ -1280,18 +1280,19 @@ __global__ void __launch_bounds__(kMcScanThreads) mc_scan_kernel(const __grid_co
     }
 }
 
-// Emission.  Warps take the listed tiles in turn (warp w of the grid: list
-// entries w, w + warps, ...; no CTA waits on another warp).  For each group
+// Emission.  Each warp takes the next listed tile from a ticket (no CTA
+// waits on another warp).  For each group
 // of 32 consecutive cubes that the count kernel marked, in cube order, a
 // warp classifies the group again (lane l: cube l; its x corners loaded, its
 // x + 1 corners the next lane's, or loaded by the lane when the next cube
-// starts a new row or lies in the next group), scans the triangle counts and
-// then emits the group's triangles 32 at a time, one triangle per lane: the
-// lane finds its cube and the triangle's place in the cube's case from a
-// per-warp slot table, takes the cube's type and corner values from the
-// owning lane by shuffles, and stages the vertices in shared memory, so that
-// the warp writes consecutive triangles with coalesced stores.
-constexpr int kMcEmitMaxPerGroup = 32 * 5;   // triangles of a group of 32 cubes, at most
+// starts a new row or lies in the next group), puts the cubes with
+// triangles (their corner values, index and case) into a per-warp ring of
+// cubes and their triangles into a per-warp queue, and writes the queue 32
+// triangles at a time, one triangle per lane, the vertices staged in shared
+// memory so that the warp stores consecutive triangles with coalesced
+// writes.  Batches run across groups; a tile's last batch may be partial.
+constexpr int kMcCubeRing = 64;    // cubes whose triangles are queued: < 32 pending + one group
+constexpr int kMcTriRing = 256;    // queued triangles: < 32 pending + up to 5 per cube of a group
 
 template <int MODE>
 __device__ __forceinline__ void mc_vertex(const McArgs& a, uint32_t cx, uint32_t cy, uint32_t cz, int64_t b0, int64_t b1,
@@ -1355,9 +1356,11 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
     __shared__ unsigned long long s_tri[256];
     __shared__ unsigned char s_ends[12];
     __shared__ unsigned char s_type[256];
-    __shared__ unsigned char s_slot[kWarps][kMcEmitMaxPerGroup];   // owner lane | triangle of its case << 5
-    __shared__ float s_out[kWarps][32 * 9];                         // a batch of 32 triangles
-    __shared__ float s_val[kWarps][8][32];                          // corner values of each lane's cube
+    __shared__ float s_cval[kWarps][8][kMcCubeRing];        // corner values of the queued cubes
+    __shared__ uint32_t s_cube[kWarps][kMcCubeRing];         // their linear index
+    __shared__ unsigned char s_ctype[kWarps][kMcCubeRing];   // their case
+    __shared__ unsigned short s_tq[kWarps][kMcTriRing];      // queued triangles: cube slot | triangle << 6
+    __shared__ float s_out[kWarps][32 * 9];                  // a batch of 32 triangles
     mc_load_tables(s_count, s_tri, s_ends, s_type);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1365,13 +1368,60 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
     constexpr uint32_t kWords = (uint32_t)mc_tile_cubes(MODE) / 1024u;   // group words per tile
     const uint32_t nwords = (a.ncubes + 1023u) / 1024u;
     const bool indexed = MODE == kFixed && a.edge_bits != nullptr;
-    const unsigned gw = blockIdx.x * kWarps + warp, nw = gridDim.x * kWarps;
-    unsigned char* slot = s_slot[warp];
+    float (*cval)[kMcCubeRing] = s_cval[warp];
+    uint32_t* cube_of = s_cube[warp];
+    unsigned char* ctype = s_ctype[warp];
+    unsigned short* tq = s_tq[warp];
     float* sout = s_out[warp];
-    float (*sval)[32] = s_val[warp];
-    for (unsigned job = gw; job < njobs; job += nw) {
+
+    // writes the queued triangles [head, head + cnt) (cnt <= 32) from output `first`
+    auto emit_batch = [&](uint32_t head, int cnt, long long first) {
+        const bool act = lane < cnt;
+        if (act) {
+            const unsigned e16 = tq[(head + (uint32_t)lane) & (kMcTriRing - 1)];
+            const int sl = (int)(e16 & 63u), tr = (int)(e16 >> 6);
+            const uint32_t cc = cube_of[sl];
+            const int t = ctype[sl];
+            const uint32_t row = fastdiv(cc, a.div_cx);
+            const uint32_t cx = cc - row * (uint32_t)(a.gx - 1);
+            const uint32_t cz = fastdiv(row, a.div_cy);
+            const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
+            int64_t b0, b1;
+            cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
+            const unsigned long long edges = s_tri[t];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int e = (int)((edges >> (4 * (3 * tr + j))) & 15ull);
+                const int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
+                if (indexed) {
+#if !defined(GBT_REF_ARITH)
+                    const long long out = first + lane;
+                    if (out < a.cap) a.tris[3 * out + j] = mc_vertex_index(a, cx, cy, cz, ca, cb);
+#endif
+                } else {
+                    mc_vertex<MODE>(a, cx, cy, cz, b0, b1, cval[ca][sl], cval[cb][sl], ca, cb, sout + 9 * lane + 3 * j);
+                }
+            }
+        }
+        __syncwarp();
+        if (!indexed) {
+            // consecutive triangles first, first + 1, ...: 9 floats and 3 indices each
+            const long long fit = a.cap - first;   // triangles of the batch that fit
+            const int nf = 9 * (int)(fit < cnt ? (fit > 0 ? fit : 0) : cnt);
+            for (int f = lane; f < nf; f += 32) a.verts[9 * first + f] = sout[f];
+            for (int f = lane; f < nf / 3; f += 32) a.tris[3 * first + f] = (int32_t)(a.index_base + 3 * first + f);
+        }
+        __syncwarp();
+    };
+
+    for (;;) {
+        unsigned job = 0;
+        if (lane == 0) job = atomicAdd(a.ticket, 1u);   // the next listed tile
+        job = __shfl_sync(0xffffffffu, job, 0);
+        if (job >= njobs) break;
         const uint32_t tile = a.tile_list[job];
-        long long out0 = (long long)a.status[tile];   // this tile's first triangle
+        long long out_next = (long long)a.status[tile];   // this tile's next triangle to write
+        uint32_t tq_head = 0, tq_tail = 0, cq_head = 0;  // (the same in every lane)
 #pragma unroll 1
         for (uint32_t w = 0; w < kWords; ++w) {
             const uint32_t word = tile * kWords + w;
@@ -1392,12 +1442,13 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
                     X[k] = __ldg(a.D + idx[k]);
                     if (MODE == kFixed) WX[k] = __ldg(a.W + idx[k]);
                 }
-                bool okn = true;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) N[k] = __shfl_down_sync(0xffffffffu, X[k], 1);
-                bool okx = true;
-                if (MODE == kFixed) okx = WX[0] > 0.f && WX[1] > 0.f && WX[2] > 0.f && WX[3] > 0.f;
-                if (MODE == kFixed) okn = __shfl_down_sync(0xffffffffu, okx ? 1 : 0, 1) != 0;
+                bool okx = true, okn = true;
+                if (MODE == kFixed) {
+                    okx = WX[0] > 0.f && WX[1] > 0.f && WX[2] > 0.f && WX[3] > 0.f;
+                    okn = __shfl_down_sync(0xffffffffu, okx ? 1 : 0, 1) != 0;
+                }
                 if (own) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
@@ -1415,6 +1466,9 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
                 int type = s_type[sx | sn << 4];
                 if (!in || (MODE == kFixed && !(okx && okn))) type = 0;
                 const int n = s_count[type];
+                // the cubes with triangles take consecutive ring slots, in cube order
+                const uint32_t act = __ballot_sync(0xffffffffu, n > 0);
+                const uint32_t rank = (uint32_t)__popc(act & ((1u << lane) - 1u));
                 int incl = n;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -1422,61 +1476,33 @@ __global__ void __launch_bounds__(kMcThreads) mc_emit_kernel(const __grid_consta
                     if (lane >= o) incl += y;
                 }
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
-                for (int k = 0; k < n; ++k) slot[incl - n + k] = (unsigned char)(lane | k << 5);
-                __syncwarp();
-                // the cube's eight corners in the reference's numbering
-                const float val[8] = {X[0], N[0], N[1], X[1], X[2], N[2], N[3], X[3]};
-                for (int base = 0; base < total; base += 32) {
-                    const int qi = base + lane;
-                    const bool act = qi < total;
-                    const int sl = act ? slot[qi] : 0;
-                    const int o = sl & 31, tr = sl >> 5;
-                    // every lane takes part in the shuffles
-                    const int t = __shfl_sync(0xffffffffu, type, o);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) sval[k][lane] = __shfl_sync(0xffffffffu, val[k], o);
-                    __syncwarp();
-                    const uint32_t cc = (uint32_t)((uint64_t)(word * 32u + g) * 32u) + (uint32_t)o;
-                    if (act) {
-                        const uint32_t row = fastdiv(cc, a.div_cx);
-                        const uint32_t cx = cc - row * (uint32_t)(a.gx - 1);
-                        const uint32_t cz = fastdiv(row, a.div_cy);
-                        const uint32_t cy = row - cz * (uint32_t)(a.gy - 1);
-                        int64_t b0, b1;
-                        cube_base<MODE>(a, cx, cy, cz, &b0, &b1);
-                        const unsigned long long edges = s_tri[t];
-#pragma unroll
-                        for (int j = 0; j < 3; ++j) {
-                            const int e = (int)((edges >> (4 * (3 * tr + j))) & 15ull);
-                            const int ca = s_ends[e] & 15, cb = s_ends[e] >> 4;
-                            if (indexed) {
-#if !defined(GBT_REF_ARITH)
-                                const long long out = out0 + qi;
-                                if (out < a.cap) a.tris[3 * out + j] = mc_vertex_index(a, cx, cy, cz, ca, cb);
-#endif
-                            } else {
-                                mc_vertex<MODE>(a, cx, cy, cz, b0, b1, sval[ca][lane], sval[cb][lane], ca, cb,
-                                                sout + 9 * lane + 3 * j);
-                            }
-                        }
-                    }
-                    __syncwarp();
-                    if (!indexed) {
-                        // consecutive triangles out0 + base ... : 9 floats and 3 indices each
-                        const int nt = min(32, total - base);
-                        const long long first = out0 + base;
-                        const long long fit = a.cap - first;          // triangles of the batch that fit
-                        const int nw9 = 9 * (int)(fit < nt ? (fit > 0 ? fit : 0) : nt);
-                        for (int f = lane; f < nw9; f += 32) a.verts[9 * first + f] = sout[f];
-                        for (int f = lane; f < nw9 / 3; f += 32)
-                            a.tris[3 * first + f] = (int32_t)(a.index_base + 3 * first + f);
-                    }
-                    __syncwarp();
+                if (n > 0) {
+                    const int sl = (int)((cq_head + rank) & (kMcCubeRing - 1));
+                    // the cube's eight corners in the reference's numbering
+                    cval[0][sl] = X[0];
+                    cval[1][sl] = N[0];
+                    cval[2][sl] = N[1];
+                    cval[3][sl] = X[1];
+                    cval[4][sl] = X[2];
+                    cval[5][sl] = N[2];
+                    cval[6][sl] = N[3];
+                    cval[7][sl] = X[3];
+                    cube_of[sl] = c;
+                    ctype[sl] = (unsigned char)type;
+                    for (int k = 0; k < n; ++k)
+                        tq[(tq_tail + (uint32_t)(incl - n + k)) & (kMcTriRing - 1)] = (unsigned short)(sl | k << 6);
                 }
-                out0 += total;
-                __syncwarp();   // the slot table is rewritten by the next group
+                cq_head += (uint32_t)__popc(act);
+                tq_tail += (uint32_t)total;
+                __syncwarp();
+                while (tq_tail - tq_head >= 32u) {
+                    emit_batch(tq_head, 32, out_next);
+                    tq_head += 32u;
+                    out_next += 32;
+                }
             }
         }
+        if (tq_tail != tq_head) emit_batch(tq_head, (int)(tq_tail - tq_head), out_next);
     }
 }
 
@@ -1789,8 +1815,6 @@ const McGrid& mc_grid() {
     return g;
 }
 
-// The four-column count kernel needs every row and layer of the distances
-// (and weights) to start on a 16-byte boundary.
 template <int MODE>
 bool mc_rows_of_4(const McArgs& a) {
     const long long layer = MODE == kCompat ? (long long)a.gx + a.gy : (long long)a.gx * a.gy;
