@@ -50,11 +50,14 @@ def parse():
     ap.add_argument("--refine-lr", type=float, default=3e-4)
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "multiscene", "diff", "refine", "points"],
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "multiscene", "diff", "refine", "points", "onepass"],
                     help="batched: one 512^3 volume, 300 frames; multiscene: 16 volumes 64^3..384^3, 10..120 frames; "
                          "diff: forward + adjoint timing and finite-difference check at 128^3 x 16 frames; "
                          "refine: 1024^3 x 1000 frames 1280x720, then pose refinement of 64 jittered frames; "
-                         "points: 30 frames 640x480 to a cloud, projected to a view")
+                         "points: 30 frames 640x480 to a cloud, projected to a view; "
+                         "onepass: the 512^3 volume, one frame per pass (the reference's calling pattern), "
+                         "every brick shape with the depth gathered and staged in shared memory")
     a = ap.parse_args()
     if a.grid is None:
         a.grid = 1024 if a.workload == "refine" else 512
@@ -932,6 +935,45 @@ def multiscene(args, torch, rank, world, local):
     }
 
 
+def onepass_workload(args, torch):
+    """One frame per pass over the full volume, as TSDFVolume::integrate is
+    called: for each brick shape, with the depth gathered from the image
+    (bricks 0-3) and staged in shared memory per warp (4-7), the mean CUDA-event
+    time of a pass over the frames of the helix (after one warm-up sweep),
+    voxel-updates/s and the algorithmic 16 B per voxel-update against the
+    measured copy bandwidth."""
+    from cuphoto import TSDFVolume
+    S, cam, scene, poses = workload(args, 0)
+    nf = len(poses)
+    nvox = args.grid ** 3
+    frames = S.render_sequence_torch(scene, poses, cam, seed=0)
+    depths = [frames[k] for k in range(nf)]
+    vol = TSDFVolume(volume_cfg(args, cam, args.mode))
+    peak, peak_kind = peaks()
+    rows = []
+    for brick in range(8):
+        def sweep():
+            vol.reset()
+            for k in range(nf):
+                vol.integrate_frames(depths[k:k + 1], poses[k:k + 1], brick=brick)
+        sweep()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sweep()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / nf
+        gbs = 16.0 * nvox / (ms * 1e-3) / 1e9
+        rows.append({"brick": brick, "depth": "staged" if brick >= 4 else "gathered", "ms_per_frame": ms,
+                     "voxel_updates_per_s": nvox / (ms * 1e-3), "algorithmic_gbs": gbs, "frac_of_peak": gbs / peak})
+    vol.close()
+    best = {d: min((r for r in rows if r["depth"] == d), key=lambda r: r["ms_per_frame"]) for d in ("gathered", "staged")}
+    return {"workload": "one frame per pass, %d^3 voxels, %d frames 640x480 uint16, %s mode" % (args.grid, nf, args.mode),
+            "peak_gbs": peak, "peak_kind": peak_kind, "rows": rows, "best": best,
+            "staged_over_gathered": best["staged"]["ms_per_frame"] / best["gathered"]["ms_per_frame"]}
+
+
 def multiscene_summary(args, torch, local):
     """The multi-scene configuration (16 seeded scenes, 64^3..384^3, 10..120
     frames, one batched launch per window, autotuned, graph-captured) run
@@ -968,6 +1010,15 @@ def main():
         spec.loader.exec_module(eb)
         eb.build()
         print(json.dumps(points_workload(args, torch)), flush=True)
+        return
+    if args.workload == "onepass":
+        import torch
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gbt_engine_build", os.path.join(PKG, "build.py"))
+        eb = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(eb)
+        eb.build()
+        print(json.dumps(onepass_workload(args, torch)), flush=True)
         return
     if args.workload == "diff":
         import torch

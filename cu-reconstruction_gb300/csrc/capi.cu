@@ -101,7 +101,7 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 // (one wave of the persistent grid), cached per kernel.
 int integrate_default_ctas_per_sm(int mode, int arith, int kind, int brick) {
     // host threads may race to fill an entry: each computes the same value
-    static std::atomic<int> cache[3][3][4] = {};
+    static std::atomic<int> cache[3][4][4] = {};
     const int k = mode == GBT_MODE_FIXED ? 2 : (arith == GBT_ARITH_IEEE ? 1 : 0);
     const int b = brick >= 0 && brick < 4 ? brick : 0;
     std::atomic<int>& slot = cache[k][kind][b];
@@ -487,7 +487,10 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     gbt_status st = check_frames(frames, nframes);
     if (st != GBT_OK) return st;
-    if (brick < 0 || brick > 3) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..3", brick);
+    if (brick < 0 || brick > 7) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..7", brick);
+    if (brick >= 4 && nframes > gbt::kLaneBrickFrames)
+        return fail(GBT_ERR_INVALID_ARG, "brick %d (depth staged in shared memory) takes passes of up to %d frames",
+                    brick, gbt::kLaneBrickFrames);
     if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(GBT_ERR_INVALID_ARG, "ctas_per_sm %d outside 0..32", ctas_per_sm);
     gbt::IntegrateArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -513,17 +516,16 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
         if (v->cfg.mode == GBT_MODE_FIXED) fixed_projection(f.pose, v->cfg, fd.P);
     }
     int bx, by, bz;
-    gbt::brick_extent(brick, &bx, &by, &bz);
+    gbt::brick_extent(brick & 3, &bx, &by, &bz);
     const uint32_t nbx = (uint32_t)((v->desc.nx + bx - 1) / bx), nby = (uint32_t)((v->desc.ny + by - 1) / by);
     const long long nbricks = (long long)nbx * nby * ((v->desc.nz + bz - 1) / bz);   // below 2^32: fewer than voxels
     a.nbricks = (uint32_t)nbricks;
     a.div_nbx = gbt::make_fastdiv(nbx);
     a.div_nby = gbt::make_fastdiv(nby);
+    const int kind = brick >= 4 ? 3 : (nframes <= gbt::kLaneBrickFrames ? 1 : 0);
     long long grid = (long long)device_sms() *
                      (ctas_per_sm ? ctas_per_sm
-                                  : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith,
-                                                                       nframes <= gbt::kLaneBrickFrames ? 1 : 0,
-                                                                       brick));
+                                  : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith, kind, brick & 3));
     if (grid > nbricks) grid = nbricks;
     if (grid < 1) grid = 1;
     cudaError_t e;

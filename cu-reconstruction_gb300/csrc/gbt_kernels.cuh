@@ -285,6 +285,94 @@ __device__ __forceinline__ void gather_depth(const FrameSlot& fs, const bool (&i
     }
 }
 
+// Depth staged in shared memory, for one warp and one frame.  The warp's
+// pixels (those of its voxels that land on the image) span a rectangle of
+// rows [vmin, vmax] and columns [umin, umax] (reductions over the warp); if
+// it fits kDepthTileBytes, the warp copies that rectangle of the image into
+// its tile with coalesced loads (8-byte chunks when the rows allow it) and
+// every voxel reads its sample from the tile; otherwise the voxels gather
+// from the image as gather_depth does.  The samples are the same values
+// either way (the same conversion of the same pixel).
+constexpr int kDepthTileBytes = 4096;
+
+__device__ __forceinline__ void gather_staged(const FrameSlot& fs, const bool (&in)[4], const int (&pu)[4],
+                                              const int (&pv)[4], const uint32_t (&pix)[4], float (&dv)[4],
+                                              unsigned char* tile) {
+    const int lane = threadIdx.x & 31;
+    int umin = 0x7fffffff, umax = -1, vmin = 0x7fffffff, vmax = -1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (in[i]) {
+            umin = min(umin, pu[i]);
+            umax = max(umax, pu[i]);
+            vmin = min(vmin, pv[i]);
+            vmax = max(vmax, pv[i]);
+        }
+    umin = __reduce_min_sync(0xffffffffu, umin);
+    umax = __reduce_max_sync(0xffffffffu, umax);
+    vmin = __reduce_min_sync(0xffffffffu, vmin);
+    vmax = __reduce_max_sync(0xffffffffu, vmax);
+    if (umax < 0) {   // no voxel of the warp lands on the image (the same for the whole warp)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dv[i] = 0.f;
+        return;
+    }
+    const bool u16 = fs.fmt != kSlotF32;
+    const int esz = u16 ? 2 : 4;
+    const int per8 = 8 / esz;   // elements per 8-byte chunk
+    // 8-byte chunks need an 8-byte aligned image and rows of whole chunks
+    const bool vec = (reinterpret_cast<uintptr_t>(fs.depth) & 7u) == 0 && (fs.pitch_elems % (uint32_t)per8) == 0;
+    const int u0 = vec ? (umin & ~(per8 - 1)) : umin;
+    const int nch = vec ? (umax - u0) / per8 + 1 : umax - umin + 1;   // chunks (or elements) per tile row
+    const int rowe = vec ? nch * per8 : nch;                          // tile row in elements
+    const int th = vmax - vmin + 1;
+    if (rowe * th * esz > kDepthTileBytes) {
+        gather_depth(fs, in, pix, dv);
+        return;
+    }
+    const unsigned char* img = static_cast<const unsigned char*>(fs.depth);
+    const int total = nch * th;
+    __syncwarp();   // the previous frame's reads of the tile are done
+    for (int k = lane; k < total; k += 32) {
+        const int r = k / nch, c = k - r * nch;
+        const size_t e = (size_t)(vmin + r) * fs.pitch_elems + (size_t)u0 + (size_t)c * (vec ? per8 : 1);
+        if (vec)
+            *reinterpret_cast<uint2*>(tile + (size_t)k * 8) = __ldg(reinterpret_cast<const uint2*>(img + e * esz));
+        else if (u16)
+            reinterpret_cast<unsigned short*>(tile)[k] = __ldg(reinterpret_cast<const unsigned short*>(img) + e);
+        else
+            reinterpret_cast<float*>(tile)[k] = __ldg(reinterpret_cast<const float*>(img) + e);
+    }
+    __syncwarp();
+    const f2 S{fs.scale2};
+    if (fs.fmt == kSlotU16Fma) {
+        uint32_t raw[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            raw[i] = in[i] ? (uint32_t)reinterpret_cast<const unsigned short*>(tile)[(pv[i] - vmin) * rowe + (pu[i] - u0)]
+                           : 0u;
+        const f2 B = f2_mul(S, f2_splat(-8388608.0f));
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            const f2 r = f2_fma(f2_pack(__uint_as_float(raw[h] | 0x4B000000u), __uint_as_float(raw[h + 1] | 0x4B000000u)),
+                                S, B);
+            dv[h] = f2_lo(r);
+            dv[h + 1] = f2_hi(r);
+        }
+    } else if (fs.fmt == kSlotU16Mul) {
+        const float scale = f2_lo(S);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            dv[i] = in[i] ? u16_metres(reinterpret_cast<const unsigned short*>(tile)[(pv[i] - vmin) * rowe + (pu[i] - u0)],
+                                       scale)
+                          : 0.f;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            dv[i] = in[i] ? reinterpret_cast<const float*>(tile)[(pv[i] - vmin) * rowe + (pu[i] - u0)] : 0.f;
+    }
+}
+
 // The thread's place in a brick and its warp's sub-box.
 template <int TX, int BY, int BZ>
 struct BrickLayout {
@@ -339,9 +427,10 @@ __device__ __forceinline__ uint32_t brick_live_frames(const VolDesc& v, const Fr
 // the fixed mode, the voxel's camera z.  Split from the update so that the
 // next frame's depth gathers are in flight while this frame's running
 // averages are computed.  FULL: the thread has all 4 voxels (nvalid == 4).
-template <int MODE, bool FULL>
+template <int MODE, bool FULL, bool STAGE = false>
 __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot& fs, const float* px, float py, float pz,
-                                              int nvalid_, float (&dv)[4], float (&zc)[4]) {
+                                              int nvalid_, float (&dv)[4], float (&zc)[4],
+                                              unsigned char* tile = nullptr) {
     const int nvalid = FULL ? 4 : nvalid_;
     // pixel (u, v) is element v * pitch_elems + u of the image (the host checks
     // that height * pitch_elems fits 32 bits and that the pitch is a whole
@@ -396,7 +485,10 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
             in[i] = i < nvalid && (uint32_t)pu[i] < width && (uint32_t)pv[i] < height;
             pix[i] = (uint32_t)pv[i] * pitch_elems + (uint32_t)pu[i];
         }
-        gather_depth(fs, in, pix, dv);
+        if (STAGE)
+            gather_staged(fs, in, pu, pv, pix, dv, tile);
+        else
+            gather_depth(fs, in, pix, dv);
     } else {
 #if !defined(GBT_REF_ARITH)
         // K [R | t] applied to voxel pairs in paired FP32 (the same rounding
@@ -408,6 +500,7 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
         const f2 p0 = f2_splat(pr[0]), p4 = f2_splat(pr[4]), p8 = f2_splat(pr[8]);
         bool in[4];
         uint32_t pix[4];
+        int pu[4], pv[4];
 #pragma unroll
         for (int h = 0; h < 4; h += 2) {
             const f2 X = f2_pack(px[h], px[h + 1]);
@@ -425,9 +518,14 @@ __device__ __forceinline__ void frame_samples(const VolDesc& v, const FrameSlot&
                 zc[i] = z;
                 in[i] = i < nvalid && z > v.min_z && (uint32_t)u < width && (uint32_t)vv < height;
                 pix[i] = (uint32_t)vv * pitch_elems + (uint32_t)u;
+                pu[i] = u;
+                pv[i] = vv;
             }
         }
-        gather_depth(fs, in, pix, dv);
+        if (STAGE)
+            gather_staged(fs, in, pu, pv, pix, dv, tile);
+        else
+            gather_depth(fs, in, pix, dv);
 #endif
     }
 }
@@ -566,14 +664,14 @@ __device__ __forceinline__ void fill_inv_table(float* s_inv) {
 }
 
 // The frames of `mask` applied one after the other (sample, then update).
-template <int MODE, bool FULL>
+template <int MODE, bool FULL, bool STAGE = false>
 __device__ __forceinline__ bool frames_in_turn(const VolDesc& v, const FrameSlot* slots, uint32_t mask,
-                                               ThreadVoxels& t, const float* s_inv) {
+                                               ThreadVoxels& t, const float* s_inv, unsigned char* tile = nullptr) {
     bool dirty = false;
     for (; mask; mask &= mask - 1) {
         const int f = __ffs(mask) - 1;
         float dv[4], zc[4];
-        frame_samples<MODE, FULL>(v, slots[f], t.px, t.py, t.pz, t.nvalid, dv, zc);
+        frame_samples<MODE, FULL, STAGE>(v, slots[f], t.px, t.py, t.pz, t.nvalid, dv, zc, tile);
         dirty |= frame_update<MODE, FULL>(v, dv, zc, t.pz, t.nvalid, t.d, t.w, s_inv);
     }
     return dirty;
@@ -583,12 +681,17 @@ __device__ __forceinline__ bool frames_in_turn(const VolDesc& v, const FrameSlot
 // per brick; longer passes with one lane per frame.  The short-pass instance
 // is latency-bound: 10 resident CTAs per SM (48 registers, a few bytes of
 // spill) beat 8 at its natural 59 registers by 2-6 %.
-template <int MODE, int TX, int BY, int BZ, bool LANE_BRICKS>
+// STAGE (lane-brick passes only): each warp stages the depth its voxels
+// sample in shared memory, frame by frame (gather_staged).
+template <int MODE, int TX, int BY, int BZ, bool LANE_BRICKS, bool STAGE = false>
 __global__ void __launch_bounds__(128, LANE_BRICKS ? 10 : 0) integrate_kernel(const __grid_constant__ IntegrateArgs a) {
     static_assert(TX * BY * BZ == 128, "128 threads per CTA");
     static_assert(32 % TX == 0, "a warp spans whole x rows");
+    static_assert(!STAGE || LANE_BRICKS, "depth staging in the lane-brick pass kernel");
     __shared__ FrameSlot s_frame[GBT_MAX_FRAMES_PER_PASS];
     __shared__ float s_inv[256];
+    __shared__ __align__(16) unsigned char s_tile[STAGE ? 4 : 1][STAGE ? kDepthTileBytes : 16];
+    unsigned char* const tile = s_tile[STAGE ? (threadIdx.x >> 5) : 0];
 
     const VolDesc& v = a.vol;
     const int tid = threadIdx.x;
@@ -613,12 +716,27 @@ __global__ void __launch_bounds__(128, LANE_BRICKS ? 10 : 0) integrate_kernel(co
     // the warp's voxels of one brick, the frames of fmask in turn
     auto process = [&](int bx0, int by0, int bz0, uint32_t fmask) {
         ThreadVoxels t;
+        if constexpr (STAGE) {
+            // every lane of the warp takes part in the staging (its reductions
+            // and shuffles): lanes past the volume's edge sample with no voxel
+            const bool ok = t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz);
+            if (ok) {
+                t.load(v);
+            } else {
+                t.nvalid = 0;
+                t.py = t.pz = 0.f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) t.px[i] = 0.f;
+            }
+            if (frames_in_turn<MODE, false, true>(v, s_frame, fmask, t, s_inv, tile) && ok) t.store(v);
+            return;
+        }
         if (t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) {
             t.load(v);
             // frame by frame: the pipelined apply_frames of the batched kernel
             // makes 32-frame passes 6.6 % slower here, at the same 9 CTAs/SM
-            const bool dirty = t.nvalid == 4 ? frames_in_turn<MODE, true>(v, s_frame, fmask, t, s_inv)
-                                             : frames_in_turn<MODE, false>(v, s_frame, fmask, t, s_inv);
+            const bool dirty = t.nvalid == 4 ? frames_in_turn<MODE, true, STAGE>(v, s_frame, fmask, t, s_inv, tile)
+                                             : frames_in_turn<MODE, false, STAGE>(v, s_frame, fmask, t, s_inv, tile);
             if (dirty) t.store(v);
         }
     };
@@ -1722,21 +1840,28 @@ __global__ void __launch_bounds__(256) weld_vertices_kernel(const __grid_constan
 
 // ---------------------------------------------------------------------------
 template <int MODE, int TX, int BY, int BZ>
-cudaError_t launch_integrate_shape(const IntegrateArgs& a, int grid, cudaStream_t s) {
-    if (a.nframes <= kLaneBrickFrames)
-        integrate_kernel<MODE, TX, BY, BZ, true><<<grid, 128, 0, s>>>(a);
-    else
+cudaError_t launch_integrate_shape(const IntegrateArgs& a, int grid, bool stage, cudaStream_t s) {
+    if (a.nframes <= kLaneBrickFrames) {
+        if (stage)
+            integrate_kernel<MODE, TX, BY, BZ, true, true><<<grid, 128, 0, s>>>(a);
+        else
+            integrate_kernel<MODE, TX, BY, BZ, true><<<grid, 128, 0, s>>>(a);
+    } else {
         integrate_kernel<MODE, TX, BY, BZ, false><<<grid, 128, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
+// brick 0-3: the four brick shapes; 4-7: the same shapes with the depth
+// staged in shared memory (passes of up to kLaneBrickFrames frames)
 template <int MODE>
 cudaError_t launch_integrate_mode(const IntegrateArgs& a, int brick, int grid, cudaStream_t s) {
-    switch (brick) {
-        case 1: return launch_integrate_shape<MODE, 4, 8, 4>(a, grid, s);
-        case 2: return launch_integrate_shape<MODE, 8, 2, 8>(a, grid, s);
-        case 3: return launch_integrate_shape<MODE, 16, 2, 4>(a, grid, s);
-        default: return launch_integrate_shape<MODE, 8, 4, 4>(a, grid, s);
+    const bool stage = brick >= 4;
+    switch (brick & 3) {
+        case 1: return launch_integrate_shape<MODE, 4, 8, 4>(a, grid, stage, s);
+        case 2: return launch_integrate_shape<MODE, 8, 2, 8>(a, grid, stage, s);
+        case 3: return launch_integrate_shape<MODE, 16, 2, 4>(a, grid, stage, s);
+        default: return launch_integrate_shape<MODE, 8, 4, 4>(a, grid, stage, s);
     }
 }
 
@@ -1769,10 +1894,12 @@ int resident_128(Kernel k) {
 }
 
 // kind: 0 the pass kernel culling one frame per lane, 1 the pass kernel
-// culling one brick per lane, 2 the batched kernel
+// culling one brick per lane, 2 the batched kernel, 3 kind 1 with the depth
+// staged in shared memory
 template <int MODE, int TX, int BY, int BZ>
 int resident_shape(int kind) {
     if (kind == 2) return resident_128(integrate_batch_kernel<MODE, TX, BY, BZ, true>);
+    if (kind == 3) return resident_128(integrate_kernel<MODE, TX, BY, BZ, true, true>);
     return kind == 1 ? resident_128(integrate_kernel<MODE, TX, BY, BZ, true>)
                      : resident_128(integrate_kernel<MODE, TX, BY, BZ, false>);
 }

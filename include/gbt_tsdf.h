@@ -163,7 +163,9 @@ gbt_status gbt_volume_transformation_voxels(gbt_volume* vol, void* stream, void*
 gbt_status gbt_integrate(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, void* stream);
 
 /* Same as gbt_integrate with an explicit tile shape and grid size, for the
- * autotuner.  brick: 0 = 32x4x4 voxels, 1 = 16x8x4, 2 = 32x2x8, 3 = 64x2x4.
+ * autotuner.  brick: 0 = 32x4x4 voxels, 1 = 16x8x4, 2 = 32x2x8, 3 = 64x2x4;
+ * 4..7 = the same shapes with each warp's depth samples staged in shared
+ * memory frame by frame (passes of up to 16 frames; same results).
  * ctas_per_sm: 0 = as many CTAs as the kernel keeps resident on an SM. */
 gbt_status gbt_integrate_tuned(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, int32_t brick,
                                int32_t ctas_per_sm, void* stream);
@@ -185,7 +187,7 @@ gbt_status gbt_integrate_tuned(gbt_volume* vol, const gbt_frame* frames, int32_t
  * records into a CUDA graph as one copy and its launches.  A replay re-reads
  * the staging area as the last call on the batch object left it, so a graph
  * should hold one call per batch object.  One host thread per batch object.
- * brick and ctas_per_sm as for gbt_integrate_tuned. */
+ * brick (0..3) and ctas_per_sm as for gbt_integrate_tuned. */
 #define GBT_MAX_FRAMES_PER_SCENE_PASS 128
 typedef struct gbt_batch gbt_batch;
 typedef struct {

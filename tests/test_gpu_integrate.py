@@ -234,3 +234,49 @@ def test_checkpoint_and_resume_is_bit_identical(gpu, tmp_path, mode):
     from cuphoto import _lib as L
     with pytest.raises(L.GbtError):
         TSDFVolume.load(str(cut))
+
+
+def _pitched(gpu, arr, extra):
+    """A device copy of the (H, W) image with `extra` unused elements after
+    each row (the kernels read it through its pitch)."""
+    h, w = arr.shape
+    host = np.zeros((h, w + extra), arr.dtype)
+    host[:, :w] = arr
+    return dev_depth(gpu, host)[:, :w]
+
+
+@pytest.mark.parametrize("k", [1, 16])
+@pytest.mark.parametrize("mode,arith,fmt", [("compat", "reference", "u16"), ("compat", "ieee", "f32"),
+                                           ("fixed", "ieee", "u16"), ("fixed", "ieee", "f32")])
+@pytest.mark.parametrize("pitch_extra", [0, 3])
+def test_depth_staged_in_shared_memory_is_bit_identical(gpu, mode, arith, fmt, k, pitch_extra):
+    """Bricks 4-7 (each warp's depth staged in shared memory) give the same
+    bits as bricks 0-3 (gathered from the image), for both sample formats,
+    rows copied in 8-byte chunks (pitch 0 extra) or element by element (a
+    pitch of 3 extra elements breaks the 8-byte row alignment), one frame and
+    16 frames per pass."""
+    from cuphoto import TSDFVolume
+    seq, tc = circle_case(n=96, frames=k, mode=mode, max_weight=8)
+    tc.arith = arith
+    imgs = list(seq.depth_u16) if fmt == "u16" else list(seq.depth_m())
+    dd = [_pitched(gpu, d, pitch_extra) for d in imgs]
+    out = {}
+    for brick in (0, 1, 2, 3, 4, 5, 6, 7):
+        vol = TSDFVolume(tc)
+        vol.integrate_frames(dd, seq.poses, depth_scale=0.001, brick=brick)
+        gpu.cuda.synchronize()
+        out[brick] = (vol.voxel_distances_data().cpu().numpy(), vol.voxel_weights_data().cpu().numpy())
+    assert (out[0][1] > 0).mean() > 0.05
+    for b in range(1, 8):
+        assert np.array_equal(out[b][1], out[0][1]), b
+        assert np.array_equal(out[b][0].view(np.uint32), out[0][0].view(np.uint32)), b
+
+
+def test_depth_staged_rejects_long_passes(gpu):
+    from cuphoto import TSDFVolume
+    from cuphoto import _lib as L
+    seq, tc = circle_case(n=32, frames=17)
+    vol = TSDFVolume(tc)
+    dd = [dev_depth(gpu, d) for d in seq.depth_u16]
+    with pytest.raises(L.GbtError, match="up to 16 frames"):
+        vol.integrate_frames(dd, seq.poses, brick=4)
