@@ -1203,23 +1203,23 @@ def main():
     frame_px = cam.width * cam.height
     alg_bytes = 16.0 * nvox + (nf / n_passes) * frame_px * 2 + (nf / n_passes) * 64
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
-    # DRAM bytes per launch: one ncu capture of integrate_batch_kernel at 320^3
-    # with a 64-frame window of 640x480 uint16 images read and wrote 274.4 +
-    # 168.2 MB (bricks no frame sees are not loaded, unchanged ones not
-    # stored).  Less the window's images read once (64 x 614.4 KB) that is
-    # 12.31 B per voxel; scaled by voxels, plus this launch's images.  The
-    # pass kernel and the fixed mode: not captured.
-    traffic = (12.31 * nvox + (nf / n_passes) * frame_px * 2) if (path == "batched" and args.mode == "compat") else None
+    # DRAM bytes and warp instructions: one ncu capture of the five
+    # integrate_batch_kernel launches of a step of this workload (512^3, 300
+    # frames in windows of 64 and 44, brick 2, resident CTAs): 4.382 GB read +
+    # 3.176 GB written and 29.94 G warp instructions for the step (bricks no
+    # frame sees are neither loaded nor stored).  Only for that launch shape;
+    # other grids, shapes and the fixed mode were not captured.
+    captured = (path == "batched" and args.mode == "compat" and args.grid == 512 and nf == 300 and K == 64)
+    traffic = (4.38248e9 + 3.17570e9) / n_passes if captured else None
     peak, peak_kind = peaks()
     # The kernel is bound by instruction issue, not by HBM (a window of K
-    # frames shares each voxel's 16 bytes).  Its issue roofline: warp
-    # instructions per voxel-update from one ncu capture of this kernel (320^3,
-    # 64-frame window: 1.604 G warp instructions for 2.097 G updates), times
-    # the measured update rate, against one instruction per clock on each of
-    # the 4 schedulers of every SM at the median SM clock sampled while timing.
+    # frames shares each voxel's 16 bytes).  Its issue roofline: the captured
+    # warp instructions per voxel-update, times the measured update rate,
+    # against one instruction per clock on each of the 4 schedulers of every
+    # SM at the median SM clock sampled while timing.
     issue = None
-    if path == "batched" and args.mode == "compat":
-        warp_inst_per_update = 1.604319e9 / (320 ** 3 * 64)
+    if captured:
+        warp_inst_per_update = 29.93774e9 / (512 ** 3 * 300)
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         sm_mhz = (clocks.summary().get("sm_mhz") or 0.0)
         upd_per_s = nvox * (nf / n_passes) / (launch_ms * 1e-3)
@@ -1228,7 +1228,7 @@ def main():
             peak_i = 4.0 * sm_count * sm_mhz * 1e6
             issue = {"unit": "warp instructions/s", "achieved": achieved_i, "peak": peak_i, "frac": achieved_i / peak_i,
                      "warp_instructions_per_update": warp_inst_per_update, "sm_mhz": sm_mhz, "sms": sm_count,
-                     "source": "instructions per update: ncu capture of integrate_batch_kernel at 320^3, 64 frames"}
+                     "source": "ncu capture of the step's integrate_batch_kernel launches at 512^3, 300 frames"}
 
     # end to end through the public API with host buffers: H2D of the step's
     # depth frames from pinned memory (on the batched path window by window,
