@@ -6,8 +6,14 @@
 //   back-projection  ((float)x - cx) * d / fx in double, rounded to float
 //                    (cuda_point_cloud.cu:44-56, K is double there);
 //   pose             float quaternion + translation (make_float4(T[1], T[2],
-//                    T[3], T[0])), R*p + t in the reference build's rounding
-//                    order (compat_geom.cuh);
+//                    T[3], T[0])); in the kernels the reference runs on the
+//                    GPU (extraction, transform) R*p + t in its device
+//                    build's rounding order (compat_geom.cuh); in the
+//                    projection, which the reference runs as a host loop,
+//                    in its host build's order: every product and sum
+//                    rounded on its own, left to right (single precision,
+//                    no fused multiply-add, as g++ -O3 compiles se3.cuh for
+//                    x86-64), checked against that loop itself;
 //   pixel            (int)((x * fx) / z + cx) in float, IEEE divide (the
 //                    reference's host loop, cuda_point_cloud.cu:262-266).
 // The z-buffer, a sequential host loop in the reference, becomes a 64-bit
@@ -54,6 +60,42 @@ __device__ __forceinline__ void apply_pose(const Pose& P, float x, float y, floa
     out[0] = compat_cam(R[0], R[1], R[2], P.t[0], x, y, z);
     out[1] = compat_cam(R[3], R[4], R[5], P.t[1], x, y, z);
     out[2] = compat_cam(R[6], R[7], R[8], P.t[2], x, y, z);
+}
+
+// The pose as the reference's host build applies it (SE3<float> from the
+// quaternion, se3.cuh:42-61,124-140, then rotate + translate, :82-95): the
+// rotation is built on the host in single precision (this file is compiled
+// with -ffp-contract=off, so each product and sum is rounded on its own),
+// and each row is ((r0 x + r1 y) + r2 z) + t with every operation rounded.
+struct HostPose {
+    float R[9];
+    float t[3];
+};
+
+HostPose make_host_pose(const double* p) {
+    const float qx = (float)p[1], qy = (float)p[2], qz = (float)p[3], qw = (float)p[0];
+    const float x = 2 * qx, y = 2 * qy, z = 2 * qz;
+    const float wx = x * qw, wy = y * qw, wz = z * qw;
+    const float xx = x * qx, xy = y * qx, xz = z * qx;
+    const float yy = y * qy, yz = z * qy, zz = z * qz;
+    HostPose h;
+    h.R[0] = 1 - (yy + zz);
+    h.R[1] = xy - wz;
+    h.R[2] = xz + wy;
+    h.R[3] = xy + wz;
+    h.R[4] = 1 - (xx + zz);
+    h.R[5] = yz - wx;
+    h.R[6] = xz - wy;
+    h.R[7] = yz + wx;
+    h.R[8] = 1 - (xx + yy);
+    h.t[0] = (float)p[4];
+    h.t[1] = (float)p[5];
+    h.t[2] = (float)p[6];
+    return h;
+}
+
+__device__ __forceinline__ float host_row(const float* r, float t, float x, float y, float z) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r[0], x), __fmul_rn(r[1], y)), __fmul_rn(r[2], z)), t);
 }
 
 // Order-preserving map of a (non-NaN) float onto unsigned integers.
@@ -145,7 +187,7 @@ struct ProjectArgs {
     const unsigned char* points;
     int64_t n;
     float fx, fy, cx, cy;
-    Pose pose;
+    HostPose pose;
     int width, height;
     unsigned long long* keys;
 };
@@ -156,7 +198,9 @@ __global__ void __launch_bounds__(kThreads) zbuffer_kernel(const __grid_constant
     float v[3];
     memcpy(v, a.points + i * kPointBytes, 12);
     float c[3];
-    apply_pose(a.pose, v[0], v[1], v[2], c);
+    c[0] = host_row(a.pose.R + 0, a.pose.t[0], v[0], v[1], v[2]);
+    c[1] = host_row(a.pose.R + 3, a.pose.t[1], v[0], v[1], v[2]);
+    c[2] = host_row(a.pose.R + 6, a.pose.t[2], v[0], v[1], v[2]);
     if (c[2] == 0.f) return;
     // a point only enters a pixel whose depth (FLT_MAX at first) exceeds its z
     if (!(c[2] < FLT_MAX)) return;
@@ -320,7 +364,7 @@ gbt_status gbt_points_project(const gbt_point* points, int64_t n, const double c
     p.fy = (float)camera_matrix[4];
     p.cx = (float)camera_matrix[2];
     p.cy = (float)camera_matrix[5];
-    p.pose = make_pose(pose);
+    p.pose = make_host_pose(pose);
     p.width = width;
     p.height = height;
     p.keys = static_cast<unsigned long long*>(scratch);

@@ -133,6 +133,39 @@ def build_ref_harness(force=False):
     return out
 
 
+def build_ref_project(force=False):
+    """The reference's host z-buffer loop (cudaPointCloud::project_to_color_depth,
+    cuda_point_cloud.cu:292-353) in an x86 host program (ref_project_main.cu),
+    compiled from the reference's sources as its Release build compiles them
+    (host code -O3, no -march: no fused multiply-adds on x86-64; device code
+    -use_fast_math -rdc=true).  Returns the program's path, or None where the
+    reference checkout is absent.  Only used to make golden vectors."""
+    exe = os.path.join(REF_OUT, "ref_project")
+    if not os.path.isdir(os.path.join(REF_ROOT, "modules")):
+        return exe if os.path.exists(exe) else None
+    main = os.path.join(HERE, "ref_project_main.cu")
+    srcs = [os.path.join(REF_ROOT, "modules/src/cuda/cuda_point_cloud.cu"), os.path.join(REF_ROOT, "modules/src/cuda/util.cu")]
+    log_src = os.path.join(REF_ROOT, "3dparty/CudaUtils/logging.cpp")
+    shims = [os.path.join(HERE, "ref_shim/opencv2/core/core.hpp"), os.path.join(HERE, "ref_shim/opencv2/core/cuda/common.hpp")]
+    if not force and not _stale(exe, srcs + [main, log_src] + shims + [__file__]):
+        return exe
+    os.makedirs(REF_OUT, exist_ok=True)
+    nvcc = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
+    inc = ["-I" + os.path.join(HERE, "ref_shim"), "-I" + os.path.join(REF_ROOT, "modules/include"),
+           "-I" + os.path.join(REF_ROOT, "modules/include/cuda"), "-I" + os.path.join(REF_ROOT, "3dparty")]
+    flags = ["-arch=sm_103a", "-use_fast_math", "-rdc=true", "-std=c++14", "-O3", "-Xcompiler", "-O3", "-w"]
+    objs = []
+    for src in srcs + [main]:
+        obj = os.path.join(REF_OUT, "host_" + os.path.basename(src) + ".o")
+        _run([nvcc] + flags + inc + ["-c", src, "-o", obj])
+        objs.append(obj)
+    log_obj = os.path.join(REF_OUT, "host_logging.o")
+    _run(["g++", "-O3", "-std=c++14", "-w", "-c", log_src, "-o", log_obj])
+    _run([nvcc, "-arch=sm_103a", "-rdc=true"] + objs + [log_obj, "-o", exe + ".tmp"])
+    os.replace(exe + ".tmp", exe)
+    return exe
+
+
 def build_all(force=False):
     out = {"oracle": build_oracle(force)}
     try:
@@ -141,6 +174,11 @@ def build_all(force=False):
         sys.stderr.write("reference cubin not built: %s\n" % e)
         out["ref_cubin"] = None
     out["ref_harness"] = build_ref_harness(force)
+    try:
+        out["ref_project"] = build_ref_project(force)
+    except Exception as e:  # optional evidence, like the cubin
+        sys.stderr.write("reference host-loop harness not built: %s\n" % e)
+        out["ref_project"] = None
     return out
 
 

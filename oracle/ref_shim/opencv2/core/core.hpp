@@ -1,11 +1,16 @@
 // Minimal stand-in for the host image type the reference's point-cloud
 // source names (cv::Mat and its small helpers), so that its CUDA kernels can
-// be compiled here for the parity checks.  Only the device code of that file
-// is used; these declarations exist so that its host functions parse.  OpenCV
-// itself is not installed in this build environment.
+// be compiled here for the parity checks, and so that its host z-buffer loop
+// (cudaPointCloud::project_to_color_depth) can run in the host-loop harness
+// (oracle/ref_project_main.cu).  A Mat is a dense row-major buffer; setTo
+// fills it; when a Mat is destroyed its size and contents are appended to
+// cv::shim_captured(), which is how the harness reads the images the loop
+// built (the loop hands them to cudaMemcpy, which has no device here).
+// OpenCV itself is not installed in this build environment.
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "cuda/common.hpp"
@@ -37,11 +42,33 @@ template <typename T, int n> struct Vec {
 };
 typedef Vec<unsigned char, 3> Vec3b;
 
+// Images of the Mats destroyed so far (see the header comment).
+struct ShimImage {
+    int rows, cols, elem;
+    std::vector<unsigned char> data;
+};
+inline std::vector<ShimImage>& shim_captured() {
+    static std::vector<ShimImage> v;
+    return v;
+}
+
 class Mat {
 public:
     Mat(Size s, int type) : rows(s.height), cols(s.width), elem(type == CV_8UC3 ? 3 : 4),
                             buf((size_t)s.width * s.height * (type == CV_8UC3 ? 3 : 4)) {}
-    template <typename T> void setTo(T) {}
+    ~Mat() { shim_captured().push_back(ShimImage{rows, cols, elem, buf}); }
+    Mat(const Mat&) = delete;
+    Mat& operator=(const Mat&) = delete;
+    // a single-channel float image: every element = v
+    void setTo(double v) {
+        const float f = (float)v;
+        for (size_t i = 0; i + 4 <= buf.size(); i += 4) std::memcpy(&buf[i], &f, 4);
+    }
+    // a three-channel 8-bit image: every pixel = the scalar's first three values
+    void setTo(const Scalar& s) {
+        for (size_t i = 0; i + 3 <= buf.size(); i += 3)
+            for (int c = 0; c < 3; ++c) buf[i + c] = (unsigned char)s.v[c];
+    }
     template <typename T> T& at(int y, int x) { return *reinterpret_cast<T*>(&buf[((size_t)y * cols + x) * elem]); }
     template <typename T> T& at(Point p) { return at<T>(p.y, p.x); }
     template <typename T> T* ptr() { return reinterpret_cast<T*>(buf.data()); }

@@ -808,13 +808,42 @@ void oracle_points_transform(uint8_t* points, int64_t n, const double* pose) {
     }
 }
 
+// The pose as the reference's host build applies it in the projection loop
+// (SE3<float>, se3.cuh:42-61,82-95,124-140): every product and sum rounded on
+// its own, left to right (this file is compiled with -ffp-contract=off; g++
+// -O3 for x86-64 emits no fused multiply-add either).
+struct HostPose {
+    float R[9], t[3];
+};
+HostPose host_pose(const double* pose) {
+    const float qx = (float)pose[1], qy = (float)pose[2], qz = (float)pose[3], qw = (float)pose[0];
+    const float x = 2 * qx, y = 2 * qy, z = 2 * qz;
+    const float wx = x * qw, wy = y * qw, wz = z * qw;
+    const float xx = x * qx, xy = y * qx, xz = z * qx;
+    const float yy = y * qy, yz = z * qy, zz = z * qz;
+    HostPose h;
+    h.R[0] = 1 - (yy + zz);
+    h.R[1] = xy - wz;
+    h.R[2] = xz + wy;
+    h.R[3] = xy + wz;
+    h.R[4] = 1 - (xx + zz);
+    h.R[5] = yz - wx;
+    h.R[6] = xz - wy;
+    h.R[7] = yz + wx;
+    h.R[8] = 1 - (xx + yy);
+    h.t[0] = (float)pose[4];
+    h.t[1] = (float)pose[5];
+    h.t[2] = (float)pose[6];
+    return h;
+}
+
 // project_to_color_depth (cuda_point_cloud.cu:292-353): the host z-buffer
 // loop in point order, then filter_image_if(FLT_MAX -> 0).  K read as
 // m[0], m[4], m[2], m[5].  The pixel is (int)((x*fx)/z + cx) in float; a
 // non-finite value is dropped.  rgb may be NULL (project_to_depth).
 void oracle_points_project(const uint8_t* points, int64_t n, const double* m, const double* pose, int32_t W,
                            int32_t H, float* depth, uint8_t* rgb) {
-    const CompatPose P = compat_pose(pose);
+    const HostPose P = host_pose(pose);
     const float fx = (float)m[0], fy = (float)m[4], cx = (float)m[2], cy = (float)m[5];
     for (int64_t i = 0; i < (int64_t)W * H; ++i) depth[i] = FLT_MAX;
     if (rgb) std::memset(rgb, 0, (size_t)W * H * 3);
@@ -822,7 +851,7 @@ void oracle_points_project(const uint8_t* points, int64_t n, const double* m, co
         const uint8_t* pt = points + i * kPointBytes;
         float p[3], c[3];
         point_pos(pt, p);
-        pose_apply(P, p, c);
+        for (int r = 0; r < 3; ++r) c[r] = P.R[3 * r] * p[0] + P.R[3 * r + 1] * p[1] + P.R[3 * r + 2] * p[2] + P.t[r];
         if (c[2] == 0.f) continue;
         const float qu = (c[0] * fx) / c[2] + cx;
         const float qv = (c[1] * fy) / c[2] + cy;

@@ -4,6 +4,7 @@ transform_points and filter_image_if kernels (bit-exact), the z-buffer
 against the reference's host loop as the oracle restates it, and the
 PointCloud mirror end to end (cloud -> colour + depth -> TSDF -> mesh)."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -191,6 +192,25 @@ def test_project_bitexact_vs_oracle(gpu, engine_lib, oracle):
     d, c = engine_project(engine_lib, gpu, pts, n, K_ROW, pose, w, h, color=False)
     ed, _ = oracle.points_project(cloud, K_ROW, pose, w, h, color=False)
     assert c is None and np.array_equal(d.view(np.uint32), ed.view(np.uint32))
+
+
+@pytest.mark.parametrize("case", ["scene", "edges"])
+def test_project_bitexact_vs_reference_host_loop(gpu, engine_lib, case):
+    """gbt_points_project against the reference's own z-buffer loop,
+    project_to_color_depth (cuda_point_cloud.cu:292-353) compiled from its
+    sources and run on the host (tests/golden/make_golden_project.py): depth
+    bits and colours identical, for a synthetic scene seen from another
+    camera and for the loop's corner cases (z = 0, points behind the camera,
+    ties, border pixels, NaN and infinite positions)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "points_project_ref.npz"))
+    cloud = g[case + "_points"]
+    w, h = (int(x) for x in g[case + "_size"])
+    pts = gpu.from_numpy(np.ascontiguousarray(cloud)).cuda()
+    d, c = engine_project(engine_lib, gpu, pts, len(cloud), g[case + "_camera_matrix"], g[case + "_pose"], w, h,
+                          pad=16)
+    assert (g[case + "_depth"] != 0).sum() > 1000
+    assert np.array_equal(d.view(np.uint32), g[case + "_depth"].view(np.uint32))
+    assert np.array_equal(c, g[case + "_color"])
 
 
 def test_filter_bitexact_vs_reference(gpu, engine_lib, oracle, ref):

@@ -144,3 +144,17 @@ def test_points_entry_points_reject_bad_arguments(engine_lib):
     assert st == L.GBT_ERR_INVALID_ARG   # more points than a 32-bit index
     assert lib.gbt_image_filter_if(None, 256, 64, 48, 0.0, 0.0, None) == L.GBT_ERR_INVALID_ARG
     assert lib.gbt_image_filter_if(dev, 100, 64, 48, 0.0, 0.0, None) == L.GBT_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("case", ["scene", "edges"])
+def test_project_oracle_against_reference_host_loop(oracle, case):
+    """The oracle's restatement of project_to_color_depth against the
+    reference's own host loop (golden vectors made by
+    tests/golden/make_golden_project.py from the reference's sources): depth
+    bits and colours identical."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "points_project_ref.npz"))
+    w, h = (int(x) for x in g[case + "_size"])
+    d, c = oracle.points_project(g[case + "_points"], g[case + "_camera_matrix"], g[case + "_pose"], w, h)
+    assert np.array_equal(d.view(np.uint32), g[case + "_depth"].view(np.uint32))
+    assert np.array_equal(c, g[case + "_color"])
