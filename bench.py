@@ -47,7 +47,10 @@ def parse():
     ap.add_argument("--refine-steps", type=int, default=50)
     ap.add_argument("--refine-frames", type=int, default=64)
     ap.add_argument("--refine-trunc", type=float, default=0.04, help="truncation (m) of the refinement volumes")
-    ap.add_argument("--refine-lr", type=float, default=3e-4)
+    ap.add_argument("--refine-lr", type=float, default=3e-4, help="Adam step (--refine-method adam)")
+    ap.add_argument("--refine-method", default="gn", choices=["gn", "adam"],
+                    help="gn: adjoint gradients preconditioned by per-frame 6x6 Gauss-Newton blocks, backtracking "
+                         "line search; adam: Adam on the se(3) left updates")
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline and reference-CUDA legs")
     ap.add_argument("--config", default="", help="brick,frames,ctas: skip the autotuner (e.g. 0,32,8)")
     ap.add_argument("--workload", default="batched",
@@ -588,6 +591,22 @@ def refine_workload(args, torch):
                 "surface_rms_mm": 1e3 * float(surf.mean().item())}
 
     before = errors(R, t)
+    if args.refine_method == "gn":
+        res = _refine_gn(args, torch, DF, dj, R, t, D0, W0, cfg, Dm, cmask, model.voxel_weights_data(), cam, tr,
+                         errors)
+        after, f_ms, b_ms, losses, extra = res
+        return {"workload": "pose refinement: %d^3 voxels of %.2f cm (FP32 D + W = %.1f GB), %d frames 1280x720 "
+                            "uint16, %d jittered frames (1 deg / 5 mm), %d Gauss-Newton steps"
+                            % (n, 256.0 / n, 8 * n ** 3 / 1e9, nf, nj, args.refine_steps),
+                "truncation_m": tr, "plain_forward": {"integrate_ms": plain_int_ms, "mesh_ms": mesh_ms,
+                                                      "triangles": int(count.item()),
+                                                      "voxel_updates_per_s": n ** 3 * nf / (plain_int_ms * 1e-3)},
+                "plain_integrate_of_jittered_frames_ms": plain64_ms,
+                "refine_step_ms": {"forward": f_ms, "forward_plus_loss_and_adjoint": b_ms,
+                                   "fwd_plus_adjoint_over_fwd": (f_ms + b_ms) / f_ms},
+                "loss": {"first": losses[0], "last": losses[-1]}, "optimizer": extra,
+                "pose_error_before": before, "pose_error_after": after,
+                "reduction": {k: 1 - after[k] / before[k] for k in before}}
     m = v = None
     fwd_ms, bwd_ms, losses = [], [], []
     for it in range(1, args.refine_steps + 1):
@@ -630,6 +649,18 @@ def refine_workload(args, torch):
             "loss": {"first": losses[0], "last": losses[-1]},
             "pose_error_before": before, "pose_error_after": after,
             "reduction": {k: 1 - after[k] / before[k] for k in before}}
+
+
+def _refine_gn(args, torch, DF, dj, R, t, D0, W0, cfg, Dm, cmask, Wm, cam, tr, errors):
+    """The refinement of cuphoto.diff.refine_poses: adjoint gradients, per-frame
+    6x6 Gauss-Newton preconditioning, backtracking line search."""
+    r = DF.refine_poses(dj, R, t, Dm, Wm, cfg, steps=args.refine_steps, D0=D0, W0=W0)
+    after = errors(r["R"], r["t"])
+    losses = r["losses"]
+    extra = {"method": "adjoint gradient, per-frame 6x6 Gauss-Newton preconditioner (frame-to-model SDF), "
+                       "backtracking line search", "forward_evaluations": r["forward_evaluations"],
+             "steps": args.refine_steps, "loss_trace": losses[:: max(1, len(losses) // 10)]}
+    return after, float(np.median(r["forward_ms"])), float(np.median(r["adjoint_ms"])), losses, extra
 
 
 def points_workload(args, torch, nframes=30, reps=5):
