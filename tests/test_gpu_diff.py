@@ -141,6 +141,7 @@ def c3_fd_check(torch, case, dphi, dtr, ddep, h=1e-4):
     (False, "pose", 1e-4, 1e-4),
     (False, "depth", 1e-4, 1e-5),
     (False, "pose", 1e-5, 1e-6),
+    (True, "pose", 1e-4, 1e-4),
     (True, "pose", 1e-5, 1e-5),
     (True, "depth", 1e-4, 1e-5),
 ])
@@ -156,7 +157,8 @@ def test_c3_adjoint_against_fp64_central_differences(gpu, smooth, which, h, tol)
     5e-9 at step 1e-5.  The ground plane alone, seen at grazing angles, is
     the harder case for the difference: its depth is a rational function of
     the pixel row with a pole at the horizon, and at step 1e-4 the
-    difference is off by ~1e-4 (measured 9.6e-5); it is checked at step 1e-5."""
+    difference is off by ~1e-4 (measured 9.6e-5, inside the 1e-4 target);
+    at step 1e-5 it agrees to 7e-10."""
     case = c3_case(smooth)
     dphi, dtr, ddep = diffcase.perturbation(case, seed=3)
     if which == "pose":
