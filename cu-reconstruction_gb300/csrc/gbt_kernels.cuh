@@ -537,6 +537,48 @@ __device__ __forceinline__ bool frame_update(const VolDesc& v, const float (&dv)
                                              int nvalid_, float* d, float* w, const float* s_inv) {
     const int nvalid = FULL ? 4 : nvalid_;
     bool dirty = false;
+#if defined(GBT_REF_ARITH)
+    if (MODE == kCompat && FULL) {
+        // The same update on voxel pairs in paired FP32: the distance to the
+        // surface, the new weight, the weighted sum d*w + tsdf (contracted to
+        // one multiply-add, as the fast-math build contracts it) and its
+        // product with the approximate reciprocal of the new weight (the
+        // fast-math division), each lane rounded and flushed as the scalar
+        // instruction would.
+        const f2 NPZ = f2_splat(-pz);
+        const f2 ONE = f2_splat(1.0f);
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            const f2 S = f2_add(f2_pack(dv[h], dv[h + 1]), NPZ);
+            bool ok[2];
+            float tsdf[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const float sdf = j ? f2_hi(S) : f2_lo(S);
+                // tsdf_volume.cu:169-176 (24 is exact in float)
+                ok[j] = dv[h + j] > 0.0f && dv[h + j] <= 24.0f && sdf >= -v.trunc;
+                tsdf[j] = fminf(sdf, v.trunc);
+            }
+            const f2 Wp = f2_pack(w[h], w[h + 1]);
+            const f2 NW = f2_add(Wp, ONE);
+            const f2 NUM = f2_fma(f2_pack(d[h], d[h + 1]), Wp, f2_pack(tsdf[0], tsdf[1]));
+            float r0, r1;
+            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(f2_lo(NW)));
+            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(f2_hi(NW)));
+            const f2 ND = f2_mul(NUM, f2_pack(r0, r1));
+            if (ok[0]) {
+                w[h] = f2_lo(NW);
+                d[h] = f2_lo(ND);
+            }
+            if (ok[1]) {
+                w[h + 1] = f2_hi(NW);
+                d[h + 1] = f2_hi(ND);
+            }
+            dirty |= ok[0] || ok[1];
+        }
+        return dirty;
+    }
+#endif
     if (MODE == kCompat) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
