@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include "gbt_internal.h"
@@ -37,6 +38,14 @@ inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 // before failing, and how many to fail after that.
 std::atomic<int64_t> g_inject_skip{0};
 std::atomic<int64_t> g_inject_fail{0};
+// streamed passes (brick 8) still to launch with their first copy held back
+std::atomic<int64_t> g_inject_hold{0};
+
+// true if this streamed pass is one that gbt_debug_inject asked to hold
+bool injected_hold() {
+    if (g_inject_hold.load() <= 0) return false;
+    return g_inject_hold.fetch_sub(1) > 0;
+}
 
 // true if this allocation is one that gbt_debug_inject asked to fail
 bool injected_alloc_failure() {
@@ -88,6 +97,11 @@ struct gbt_volume {
     // shared-vertex mesh scratch: used-edge bits, word offsets, block sums, vertex count
     void* weld_scratch;
     size_t weld_scratch_bytes;
+    // status word (gbt::kStatus*), in the distances' allocation after the last distance
+    unsigned int* status;
+    // the distances and weights as tensors of the Tensor Memory Accelerator (streamed passes)
+    bool maps_ready;
+    gbt::VolumeMaps maps;
 };
 
 namespace gbt {
@@ -101,9 +115,10 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 // (one wave of the persistent grid), cached per kernel.
 int integrate_default_ctas_per_sm(int mode, int arith, int kind, int brick) {
     // host threads may race to fill an entry: each computes the same value
-    static std::atomic<int> cache[3][4][4] = {};
+    static std::atomic<int> cache[3][5][4] = {};   // [arithmetic][kind 0..4][brick shape]
     const int k = mode == GBT_MODE_FIXED ? 2 : (arith == GBT_ARITH_IEEE ? 1 : 0);
     const int b = brick >= 0 && brick < 4 ? brick : 0;
+    if (kind < 0 || kind > 4) kind = 0;
     std::atomic<int>& slot = cache[k][kind][b];
     int n = slot.load(std::memory_order_relaxed);
     if (n == 0) {
@@ -191,7 +206,49 @@ gbt_status check_frames(const gbt_frame* frames, int32_t nframes) {
     return GBT_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (the library
+// does not link the driver library itself); null if the driver has none
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
 }  // namespace
+
+// The volume's distances and weights as 3-D tensors of floats ([nz][ny][nx],
+// rows of nx * 4 bytes: nx a multiple of 4) in boxes of one streamed brick,
+// encoded once per volume (the arrays never move).
+static gbt_status volume_maps(gbt_volume* v) {
+    if (v->maps_ready) return GBT_OK;
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return fail(GBT_ERR_CUDA, "the driver has no cuTensorMapEncodeTiled");
+    const gbt::VolDesc& d = v->desc;
+    const cuuint64_t dims[3] = {(cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)d.nx * 4u, (cuuint64_t)d.nx * (cuuint64_t)d.ny * 4u};
+    const cuuint32_t box[3] = {gbt::kStreamBrickX, gbt::kStreamBrickY, gbt::kStreamBrickZ};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    float* arrays[2] = {d.D, d.W};
+    CUtensorMap* maps[2] = {&v->maps.d, &v->maps.w};
+    for (int i = 0; i < 2; ++i) {
+        // boxes past the volume's end read zeros (never stored)
+        const CUresult r = encode(maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, arrays[i], dims, strides, box, elem,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(GBT_ERR_CUDA, "cuTensorMapEncodeTiled for the volume failed (%d)", (int)r);
+    }
+    v->maps_ready = true;
+    return GBT_OK;
+}
 
 extern "C" {
 
@@ -204,12 +261,17 @@ gbt_status gbt_debug_inject(int32_t what, int64_t skip, int64_t count) {
         case GBT_INJECT_NONE:
             g_inject_fail.store(0);
             g_inject_skip.store(0);
+            g_inject_hold.store(0);
             return GBT_OK;
         case GBT_INJECT_ALLOC:
             if (skip < 0 || count < 0) return fail(GBT_ERR_INVALID_ARG, "gbt_debug_inject: negative skip or count");
             g_inject_fail.store(0);
             g_inject_skip.store(skip);
             g_inject_fail.store(count);
+            return GBT_OK;
+        case GBT_INJECT_HOLD_COPY:
+            if (count < 0) return fail(GBT_ERR_INVALID_ARG, "gbt_debug_inject: negative count");
+            g_inject_hold.store(count);
             return GBT_OK;
         case GBT_INJECT_LAUNCH_ERROR:
             // a block of zero threads: the runtime refuses the launch on the
@@ -282,14 +344,17 @@ gbt_status gbt_volume_create(const gbt_volume_cfg* cfg, void* stream, gbt_volume
     d.cy = c.cy;
 
     const size_t bytes = (size_t)nvox * sizeof(float);
+    // the status word sits 256-byte aligned after the distances
+    const size_t status_at = (bytes + 255) / 256 * 256;
     cudaError_t e;
     if (v->managed) {
-        e = dev_alloc(reinterpret_cast<void**>(&d.D), bytes, true);
+        e = dev_alloc(reinterpret_cast<void**>(&d.D), status_at + 256, true);
         if (e == cudaSuccess) e = dev_alloc(reinterpret_cast<void**>(&d.W), bytes, true);
     } else {
-        e = dev_alloc(reinterpret_cast<void**>(&d.D), bytes);
+        e = dev_alloc(reinterpret_cast<void**>(&d.D), status_at + 256);
         if (e == cudaSuccess) e = dev_alloc(reinterpret_cast<void**>(&d.W), bytes);
     }
+    if (e == cudaSuccess) v->status = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(d.D) + status_at);
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (d.D) cudaFree(d.D);
@@ -328,7 +393,25 @@ gbt_status gbt_volume_reset(gbt_volume* v, void* stream) {
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     cudaGetLastError();  // a launch reports only its own failure
     cudaError_t e = gbt::launch_volume_init(v->desc.D, v->desc.W, v->nvox, v->desc.trunc, as_stream(stream));
+    if (e == cudaSuccess) e = cudaMemsetAsync(v->status, 0, sizeof(unsigned int), as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "volume initialisation");
+    return GBT_OK;
+}
+
+gbt_status gbt_volume_check(gbt_volume* v, void* stream) {
+    gbt::TraceRange trace_("gbt_volume_check");
+    if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
+    unsigned int word = 0;
+    cudaError_t e = cudaStreamSynchronize(as_stream(stream));
+    if (e == cudaSuccess) e = cudaMemcpy(&word, v->status, sizeof(word), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "gbt_volume_check");
+    if (word & gbt::kStatusWaitExpired) {
+        e = cudaMemset(v->status, 0, sizeof(word));
+        if (e != cudaSuccess) return cuda_fail(e, "gbt_volume_check");
+        return fail(GBT_ERR_TIMEOUT,
+                    "a streamed integrate pass gave up waiting for a copy of the volume's bricks: the volume's "
+                    "distances and weights are undefined until it is reset or loaded");
+    }
     return GBT_OK;
 }
 
@@ -487,10 +570,18 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     if (!v) return fail(GBT_ERR_INVALID_ARG, "volume is NULL");
     gbt_status st = check_frames(frames, nframes);
     if (st != GBT_OK) return st;
-    if (brick < 0 || brick > 7) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..7", brick);
+    if (brick < 0 || brick > 8) return fail(GBT_ERR_INVALID_ARG, "brick %d outside 0..8", brick);
     if (brick >= 4 && nframes > gbt::kLaneBrickFrames)
-        return fail(GBT_ERR_INVALID_ARG, "brick %d (depth staged in shared memory) takes passes of up to %d frames",
-                    brick, gbt::kLaneBrickFrames);
+        return fail(GBT_ERR_INVALID_ARG, "brick %d (%s) takes passes of up to %d frames", brick,
+                    brick == 8 ? "streamed through the Tensor Memory Accelerator" : "depth staged in shared memory",
+                    gbt::kLaneBrickFrames);
+    if (brick == 8) {
+        if (v->desc.nx % 4 != 0)
+            return fail(GBT_ERR_INVALID_ARG, "brick 8 (streamed) needs an x extent that is a multiple of 4, not %d",
+                        v->desc.nx);
+        st = volume_maps(v);
+        if (st != GBT_OK) return st;
+    }
     if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(GBT_ERR_INVALID_ARG, "ctas_per_sm %d outside 0..32", ctas_per_sm);
     gbt::IntegrateArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -515,14 +606,15 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
         fd.t[2] = (float)f.pose[6];
         if (v->cfg.mode == GBT_MODE_FIXED) fixed_projection(f.pose, v->cfg, fd.P);
     }
-    int bx, by, bz;
-    gbt::brick_extent(brick & 3, &bx, &by, &bz);
+    int bx = gbt::kStreamBrickX, by = gbt::kStreamBrickY, bz = gbt::kStreamBrickZ;   // brick 8
+    if (brick != 8) gbt::brick_extent(brick & 3, &bx, &by, &bz);
     const uint32_t nbx = (uint32_t)((v->desc.nx + bx - 1) / bx), nby = (uint32_t)((v->desc.ny + by - 1) / by);
     const long long nbricks = (long long)nbx * nby * ((v->desc.nz + bz - 1) / bz);   // below 2^32: fewer than voxels
     a.nbricks = (uint32_t)nbricks;
     a.div_nbx = gbt::make_fastdiv(nbx);
     a.div_nby = gbt::make_fastdiv(nby);
-    const int kind = brick >= 4 ? 3 : (nframes <= gbt::kLaneBrickFrames ? 1 : 0);
+    a.status = v->status;
+    const int kind = brick == 8 ? 4 : (brick >= 4 ? 3 : (nframes <= gbt::kLaneBrickFrames ? 1 : 0));
     long long grid = (long long)device_sms() *
                      (ctas_per_sm ? ctas_per_sm
                                   : gbt::integrate_default_ctas_per_sm(v->cfg.mode, v->cfg.arith, kind, brick & 3));
@@ -530,7 +622,15 @@ gbt_status gbt_integrate_tuned(gbt_volume* v, const gbt_frame* frames, int32_t n
     if (grid < 1) grid = 1;
     cudaError_t e;
     cudaGetLastError();  // a launch reports only its own failure
-    if (v->cfg.mode == GBT_MODE_FIXED)
+    if (brick == 8) {
+        a.hold_first_copy = injected_hold() ? 1 : 0;
+        if (v->cfg.mode == GBT_MODE_FIXED)
+            e = gbt::launch_stream_fixed(a, v->maps, (int)grid, as_stream(stream));
+        else if (v->cfg.arith == GBT_ARITH_IEEE)
+            e = gbt::launch_stream_compat_ieee(a, v->maps, (int)grid, as_stream(stream));
+        else
+            e = gbt::launch_stream_compat_ref(a, v->maps, (int)grid, as_stream(stream));
+    } else if (v->cfg.mode == GBT_MODE_FIXED)
         e = gbt::launch_integrate_fixed(a, brick, (int)grid, as_stream(stream));
     else if (v->cfg.arith == GBT_ARITH_IEEE)
         e = gbt::launch_integrate_compat_ieee(a, brick, (int)grid, as_stream(stream));

@@ -2,6 +2,7 @@
 // and the host-side launchers each kernel TU exports.  Not part of the ABI.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
@@ -93,8 +94,23 @@ struct IntegrateArgs {
     uint32_t nbricks;        // bricks of the volume for the launch's brick shape
     FastDiv div_nbx;         // bricks along x
     FastDiv div_nby;         // bricks along y
+    unsigned int* status;    // streamed pass: the volume's status word (kStatusWaitExpired)
+    int32_t hold_first_copy; // streamed pass, failure injection: CTA 0 issues no copy for its first brick
+    int32_t pad1;
     FrameDesc frames[GBT_MAX_FRAMES_PER_PASS];
 };
+
+// The volume's distances and weights as two tensors of the Tensor Memory
+// Accelerator ([nz][ny][nx] float, x fastest; a box is one brick of the
+// streamed pass kernel, 32 x 4 x 4 voxels).
+struct alignas(128) VolumeMaps {
+    CUtensorMap d, w;
+};
+// Brick of the streamed pass kernel and the stages of its shared-memory ring.
+constexpr int kStreamBrickX = 32, kStreamBrickY = 4, kStreamBrickZ = 4;
+constexpr int kStreamStages = 4;
+// Bits of a volume's status word (a device word after its weights).
+constexpr unsigned kStatusWaitExpired = 1u;   // a bounded wait of a kernel gave up; the volume is invalid
 
 // Many volumes in one launch.  A scene's bricks are numbered from
 // brick_begin; frames [first_frame, first_frame + nframes) of the frame table
@@ -232,7 +248,8 @@ cudaError_t launch_weld_vertices_fixed(const WeldArgs& a, cudaStream_t s);
 // Batched integrate (one persistent launch over many volumes).
 cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 // CTAs per SM that the (batched or pass) integrate kernel of a brick shape keeps resident.
-// kind: 0 pass kernel culling a frame per lane, 1 pass kernel culling a brick per lane, 2 batched kernel.
+// kind: 0 pass kernel culling a frame per lane, 1 pass kernel culling a brick per lane, 2 batched kernel,
+// 3 kind 1 with the depth staged in shared memory, 4 the streamed pass kernel (brick ignored).
 int integrate_resident_ctas_compat_ref(int kind, int brick);
 int integrate_resident_ctas_compat_ieee(int kind, int brick);
 int integrate_resident_ctas_fixed(int kind, int brick);
@@ -240,6 +257,12 @@ int integrate_resident_ctas_fixed(int kind, int brick);
 constexpr int kLaneBrickFrames = 16;
 cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s);
 cudaError_t launch_batch_fixed(const BatchArgs& a, int brick, int grid, cudaStream_t s);
+// Passes of up to kLaneBrickFrames frames whose bricks' distances and weights
+// are streamed into shared memory by the Tensor Memory Accelerator (brick 8).
+// kind 4 of integrate_resident_ctas_* is this kernel.
+cudaError_t launch_stream_compat_ref(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s);
+cudaError_t launch_stream_compat_ieee(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s);
+cudaError_t launch_stream_fixed(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s);
 // k_util.cu: volume initialisation and the packed per-voxel transform records.
 cudaError_t launch_volume_init(float* D, float* W, int64_t n, float trunc, cudaStream_t s);
 cudaError_t launch_tvoxels(void* out, const VolDesc& v, cudaStream_t s);

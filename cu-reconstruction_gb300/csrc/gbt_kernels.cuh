@@ -681,6 +681,10 @@ struct ThreadVoxels {
                 w[i] = (i < nvalid) ? v.W[base + i] : 0.f;
             }
         }
+        centres(v);
+    }
+    // the voxels' world coordinates
+    __device__ __forceinline__ void centres(const VolDesc& v) {
         py = centre(y, v.vs[1], v.off[1]);
         pz = centre(z, v.vs[2], v.off[2]);
 #pragma unroll
@@ -811,6 +815,216 @@ __global__ void __launch_bounds__(128, LANE_BRICKS ? 10 : 0) integrate_kernel(co
             origin(b, bx0, by0, bz0);
             const uint32_t fmask = warp_live_frames<MODE>(v, s_frame, 0, nf, L, bx0, by0, bz0);
             if (fmask != 0u) process(bx0, by0, bz0, fmask);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Passes of up to kLaneBrickFrames frames with the distances and weights
+// streamed into shared memory by the Tensor Memory Accelerator (brick 8).
+//
+// A CTA of 128 threads takes bricks of 32 x 4 x 4 voxels (rows of 128
+// bytes); it culls its bricks 128 at a time (a thread per brick, every frame
+// of the pass), queues the live ones, and one thread keeps the copies of the
+// next kStreamStages queued bricks in flight: two tensor copies per brick
+// (its distances and its weights, 2 KB each) into a ring of shared-memory
+// stages, each stage completing on its own mbarrier.  Every thread then reads
+// its 4 voxels from the stage, the stage goes back to the copier, and the
+// thread applies the frames and stores the voxels that changed straight from
+// its registers.  The arithmetic is frames_in_turn's: the volumes are those
+// of the gathering pass kernel, bit for bit.
+//
+// With no voxel data held in registers while in flight, the distance and
+// weight loads leave the per-brick chain.  On one frame per pass at 512^3
+// that is not what bounds the gathering kernel, whose direct 16-byte loads
+// already overlap the projection and the depth gathers: this form takes
+// 0.239 ms per frame against 0.214 (its per-brick barrier ties the CTA's
+// four warps together), and a stream per warp over slabs of 32 x 4 x 1
+// voxels with the next slab's depth samples gathered before the current
+// slab's update took 0.356 ms (40 % more instructions in culling and copy
+// management per voxel).  It stays selectable for the autotuner.
+//
+// Waits are bounded: a stage whose copy does not arrive within about a second
+// sets kStatusWaitExpired in the volume's status word; the CTA then waits
+// (bounded again) for its other copies in flight and returns.
+
+constexpr int kStreamQueue = 256;              // live bricks culled and not yet applied (a ring)
+constexpr long long kWaitCycles = 1ll << 31;   // about a second at the SM clock
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// Makes the initialised barriers visible to the copy engine.
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Arrives once on `bar` and adds `bytes` to the bytes its phase waits for.
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Waits until the phase of `bar` with parity `parity` has completed; false if
+// it has not after kWaitCycles SM cycles.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint32_t parity) {
+    const uint32_t addr = smem_u32(bar);
+    long long t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (it == 0)
+            t0 = clock64();
+        else if (clock64() - t0 > kWaitCycles)
+            return false;
+    }
+}
+// Box (x, y, z) of the tensor `map` into shared memory at `dst`, completing
+// on `bar`.  x * 4 bytes is a multiple of 16 (x is a multiple of 32).
+__device__ __forceinline__ void tma_load_box3(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                              unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) integrate_stream_kernel(const __grid_constant__ IntegrateArgs a,
+                                                               const __grid_constant__ VolumeMaps maps) {
+    constexpr int TX = kStreamBrickX / 4, BY = kStreamBrickY, BZ = kStreamBrickZ;
+    static_assert(TX * BY * BZ == 128, "a thread per 4 voxels of the brick");
+    constexpr int kBrickVoxels = kStreamBrickX * BY * BZ;
+    constexpr uint32_t kStageBytes = 2u * kBrickVoxels * sizeof(float);
+    constexpr int S = kStreamStages;
+    // stage s: the brick's distances, then its weights, each [z][y][x] as the copy lays them out
+    __shared__ __align__(128) float s_dw[S][2][kBrickVoxels];
+    __shared__ __align__(8) unsigned long long s_full[S];
+    __shared__ FrameSlot s_frame[kLaneBrickFrames];
+    __shared__ float s_inv[256];
+    __shared__ uint32_t s_qbrick[kStreamQueue];
+    __shared__ uint16_t s_qmask[kStreamQueue];
+    __shared__ uint32_t s_wcount[4];
+
+    const VolDesc& v = a.vol;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nf = a.nframes;
+    if (tid < nf) load_slot<MODE>(a.frames[tid], s_frame[tid]);
+    if (MODE == kFixed) fill_inv_table(s_inv);
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) mbar_init(&s_full[st], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    const BrickLayout<TX, BY, BZ> L(tid);
+    const uint32_t nbx = a.div_nbx.d, nby = a.div_nby.d;
+    auto origin = [&](uint32_t b, int& bx0, int& by0, int& bz0) {
+        const uint32_t rest = fastdiv(b, a.div_nbx);
+        const uint32_t bzi = fastdiv(rest, a.div_nby);
+        bx0 = (int)(b - rest * nbx) * kStreamBrickX;
+        by0 = (int)(rest - bzi * nby) * BY;
+        bz0 = (int)bzi * BZ;
+    };
+    // the CTA's bricks are blockIdx.x + k * gridDim.x, k < nk; the counters
+    // below are the same in every thread
+    const uint32_t nk = a.nbricks > blockIdx.x ? (a.nbricks - blockIdx.x - 1) / gridDim.x + 1 : 0u;
+    uint32_t culled = 0;   // k of the next brick to cull
+    uint32_t qt = 0;       // live bricks queued
+    uint32_t ld = 0;       // of them, copies issued
+    uint32_t cs = 0;       // of them, applied
+
+    // culls the next 128 bricks (a thread each) and queues the live ones in order
+    auto cull = [&]() {
+        const uint32_t k = culled + (uint32_t)tid;
+        uint32_t fm = 0u, b = 0u;
+        if (k < nk) {
+            b = blockIdx.x + k * gridDim.x;
+            int bx0, by0, bz0;
+            origin(b, bx0, by0, bz0);
+            const int xh = min(bx0 + kStreamBrickX, v.nx) - 1, yh = min(by0 + BY, v.ny) - 1,
+                      zh = min(bz0 + BZ, v.nz) - 1;
+            for (int f = 0; f < nf; ++f)
+                if (!box_culled<MODE>(v, s_frame[f], bx0, xh, by0, yh, bz0, zh)) fm |= 1u << f;
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, fm != 0u);
+        if (lane == 0) s_wcount[warp] = (uint32_t)__popc(bal);
+        __syncthreads();
+        uint32_t off = 0u, tot = 0u;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t c = s_wcount[w];
+            off += w < warp ? c : 0u;
+            tot += c;
+        }
+        if (fm) {
+            const uint32_t q = (qt + off + (uint32_t)__popc(bal & ((1u << lane) - 1u))) % kStreamQueue;
+            s_qbrick[q] = b;
+            s_qmask[q] = (uint16_t)fm;
+        }
+        __syncthreads();   // the queue entries are visible, s_wcount may be written again
+        qt += tot;
+        culled += 128u;
+    };
+    // keeps up to S copies in flight (thread 0 issues them)
+    auto issue = [&]() {
+        for (; ld < qt && ld - cs < (uint32_t)S; ++ld) {
+            if (tid == 0) {
+                const uint32_t b = s_qbrick[ld % kStreamQueue];
+                int bx0, by0, bz0;
+                origin(b, bx0, by0, bz0);
+                const int st = (int)(ld % S);
+                if (a.hold_first_copy && blockIdx.x == 0 && ld == 0) continue;   // failure injection
+                mbar_arrive_expect(&s_full[st], kStageBytes);
+                tma_load_box3(s_dw[st][0], &maps.d, bx0, by0, bz0, &s_full[st]);
+                tma_load_box3(s_dw[st][1], &maps.w, bx0, by0, bz0, &s_full[st]);
+            }
+        }
+    };
+
+    while (ld == qt && culled < nk) cull();
+    issue();
+    while (cs < qt) {
+        const int st = (int)(cs % S);
+        const uint32_t parity = (cs / S) & 1u;
+        const uint32_t b = s_qbrick[cs % kStreamQueue];
+        const uint32_t fmask = s_qmask[cs % kStreamQueue];
+        const bool arrived = mbar_wait_bounded(&s_full[st], parity);
+        float4 d4 = make_float4(0.f, 0.f, 0.f, 0.f), w4 = d4;
+        if (arrived) {
+            // thread (tx, ty, tz) holds voxels 4 tx .. 4 tx + 3 of row (ty, tz): float4 number tid
+            d4 = reinterpret_cast<const float4*>(s_dw[st][0])[tid];
+            w4 = reinterpret_cast<const float4*>(s_dw[st][1])[tid];
+        }
+        // every thread has read the stage: it can take the next copy
+        if (__syncthreads_or(!arrived)) {
+            if (tid == 0) atomicOr(a.status, kStatusWaitExpired);
+            // the copies still in flight land before the CTA leaves
+            for (uint32_t u = cs + 1u; u < ld; ++u) mbar_wait_bounded(&s_full[u % S], (u / S) & 1u);
+            return;
+        }
+        ++cs;
+        while (ld == qt && culled < nk) cull();
+        issue();
+
+        int bx0, by0, bz0;
+        origin(b, bx0, by0, bz0);
+        ThreadVoxels t;
+        if (t.init(v, bx0 + 4 * L.tx, by0 + L.ty, bz0 + L.tz)) {
+            t.d[0] = d4.x; t.d[1] = d4.y; t.d[2] = d4.z; t.d[3] = d4.w;
+            t.w[0] = w4.x; t.w[1] = w4.y; t.w[2] = w4.z; t.w[3] = w4.w;
+            t.centres(v);
+            // the host launches this kernel for x extents that are multiples of 4: 4 voxels per thread
+            if (frames_in_turn<MODE, true>(v, s_frame, fmask, t, s_inv)) t.store(v);
         }
     }
 }
@@ -1907,6 +2121,12 @@ cudaError_t launch_integrate_mode(const IntegrateArgs& a, int brick, int grid, c
     }
 }
 
+template <int MODE>
+cudaError_t launch_stream_mode(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s) {
+    integrate_stream_kernel<MODE><<<grid, 128, 0, s>>>(a, m);
+    return cudaGetLastError();
+}
+
 template <int MODE, int TX, int BY, int BZ>
 cudaError_t launch_batch_shape(const BatchArgs& a, int grid, cudaStream_t s) {
     if (a.rows_of_4)
@@ -1937,7 +2157,7 @@ int resident_128(Kernel k) {
 
 // kind: 0 the pass kernel culling one frame per lane, 1 the pass kernel
 // culling one brick per lane, 2 the batched kernel, 3 kind 1 with the depth
-// staged in shared memory
+// staged in shared memory (4, the streamed pass kernel: resident_ctas_mode)
 template <int MODE, int TX, int BY, int BZ>
 int resident_shape(int kind) {
     if (kind == 2) return resident_128(integrate_batch_kernel<MODE, TX, BY, BZ, true>);
@@ -1948,6 +2168,7 @@ int resident_shape(int kind) {
 
 template <int MODE>
 int resident_ctas_mode(int kind, int brick) {
+    if (kind == 4) return resident_128(integrate_stream_kernel<MODE>);
     switch (brick) {
         case 1: return resident_shape<MODE, 4, 8, 4>(kind);
         case 2: return resident_shape<MODE, 8, 2, 8>(kind);

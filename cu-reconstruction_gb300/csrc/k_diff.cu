@@ -248,16 +248,22 @@ constexpr int kBackThreads = 128;
 // independently, so warps with little work do not hold up the others).  The
 // chunk's per-frame (D, W) history sits in shared memory, so the frame loops
 // need no unrolling.  Pose sums: per warp and frame the 12 values are reduced
-// across the warp in T and added into the CTA's shared accumulators in T;
-// the CTA's last warp to finish adds the non-zero totals into grad_pose in
-// double (no end-of-CTA barrier: finished warps leave at once).
+// across the warp in T and added into the CTA's shared accumulators in
+// double.  In the float instance the sum of the four warps' float totals is
+// then exact unless their magnitudes differ by more than 2^29, so it does not
+// depend on the order in which the warps arrive (float accumulators did: pose
+// refinement, whose line search branches on the loss, then took different
+// paths from run to run); what still depends on the order is the last bit of
+// grad_pose's double sums over CTAs.  The CTA's last warp to finish adds the
+// non-zero totals into grad_pose (no end-of-CTA barrier: finished warps
+// leave at once).
 template <typename T>
 __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, const T* gD_in, const T* gW_in,
                                                                 const T* D0, const T* W0, const T* ckpt,
                                                                 const T* depth, const T* rot, const T* trans,
                                                                 T* grad_depth, double* grad_pose, T* gD0, T* gW0) {
     __shared__ T s_pose[kBatchMaxFrames][12];
-    __shared__ T s_acc[kBatchMaxFrames][12];
+    __shared__ double s_acc[kBatchMaxFrames][12];
     __shared__ T s_hist[2 * kChunk][kBackThreads];   // D then W before each frame of the chunk
     __shared__ int s_done;                           // warps finished
     using O = Ops<T>;
@@ -276,7 +282,7 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
         return;
     }
     load_poses<T>(g, rot, trans, s_pose);
-    for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) s_acc[e / 12][e % 12] = (T)0;
+    for (int e = threadIdx.x; e < g.nframes * 12; e += kBackThreads) s_acc[e / 12][e % 12] = 0.0;
     if (threadIdx.x == 0) s_done = 0;
     __syncthreads();
     const int64_t frame = (int64_t)g.width * g.height;
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
                 acc[9] = gcx; acc[10] = gcy; acc[11] = gcz;
             }
             const T tot = warp_sum12<T>(acc, lane);
-            if (!(lane & 1) && lane < 24 && tot != (T)0) atomicAdd(&s_acc[f][lane >> 1], tot);
+            if (!(lane & 1) && lane < 24 && tot != (T)0) atomicAdd(&s_acc[f][lane >> 1], (double)tot);
         }
     }
     if (inside && gD0) gD0[i] = gd;
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(kBackThreads) backward_kernel(Geometry g, cons
     if (!__shfl_sync(0xffffffffu, last, 0)) return;
     __threadfence_block();
     for (int e = lane; e < g.nframes * 12; e += 32) {
-        const double v = (double)s_acc[e / 12][e % 12];
+        const double v = s_acc[e / 12][e % 12];
         if (v != 0.0) atomicAdd(grad_pose + e, v);
     }
 }

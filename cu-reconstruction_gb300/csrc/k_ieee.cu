@@ -16,6 +16,14 @@ cudaError_t launch_integrate_fixed(const IntegrateArgs& a, int brick, int grid, 
     return launch_integrate_mode<kFixed>(a, brick, grid, s);
 }
 
+cudaError_t launch_stream_compat_ieee(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s) {
+    return launch_stream_mode<kCompat>(a, m, grid, s);
+}
+
+cudaError_t launch_stream_fixed(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s) {
+    return launch_stream_mode<kFixed>(a, m, grid, s);
+}
+
 cudaError_t launch_batch_compat_ieee(const BatchArgs& a, int brick, int grid, cudaStream_t s) {
     return launch_batch_mode<kCompat>(a, brick, grid, s);
 }

@@ -12,6 +12,10 @@ cudaError_t launch_integrate_compat_ref(const IntegrateArgs& a, int brick, int g
     return refarith::launch_integrate_mode<refarith::kCompat>(a, brick, grid, s);
 }
 
+cudaError_t launch_stream_compat_ref(const IntegrateArgs& a, const VolumeMaps& m, int grid, cudaStream_t s) {
+    return refarith::launch_stream_mode<refarith::kCompat>(a, m, grid, s);
+}
+
 cudaError_t launch_batch_compat_ref(const BatchArgs& a, int brick, int grid, cudaStream_t s) {
     return refarith::launch_batch_mode<refarith::kCompat>(a, brick, grid, s);
 }

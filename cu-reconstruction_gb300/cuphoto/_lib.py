@@ -33,6 +33,8 @@ MAX_FRAMES_PER_PASS = 32
 INJECT_NONE = 0
 INJECT_ALLOC = 1
 INJECT_LAUNCH_ERROR = 2
+INJECT_HOLD_COPY = 3
+BRICK_STREAMED = 8
 
 
 class VolumeCfg(C.Structure):
@@ -121,6 +123,7 @@ SIGNATURES = [
     ("gbt_volume_create", C.c_int, [C.POINTER(VolumeCfg), C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_volume_destroy", C.c_int, [C.c_void_p]),
     ("gbt_volume_reset", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("gbt_volume_check", C.c_int, [C.c_void_p, C.c_void_p]),
     ("gbt_volume_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     ("gbt_volume_load", C.c_int, [C.c_char_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("gbt_volume_get_cfg", C.c_int, [C.c_void_p, C.POINTER(VolumeCfg)]),

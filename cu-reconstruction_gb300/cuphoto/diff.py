@@ -245,7 +245,8 @@ def gauss_newton_blocks(D_model, W_model, depth, R, t, cfg, stride=4):
     return H
 
 
-def refine_poses(depth, R, t, D_model, W_model, cfg, steps=50, blocks_every=10, damping=1e-3, D0=None, W0=None):
+def refine_poses(depth, R, t, D_model, W_model, cfg, steps=50, blocks_every=10, damping=1e-3, D0=None, W0=None,
+                 max_step=0.01, armijo=1e-4):
     """Refines the world-to-camera poses (R [F, 3, 3], t [F, 3]) of the depth
     frames [F, H, W] against a model volume.  Each step integrates the frames
     into a fresh volume (the differentiable forward) and evaluates
@@ -256,7 +257,13 @@ def refine_poses(depth, R, t, D_model, W_model, cfg, steps=50, blocks_every=10, 
     (gauss_newton_blocks, recomputed every `blocks_every` steps,
     Levenberg-damped by `damping` times its mean diagonal); the step length
     is found by backtracking on L from twice the last accepted length (the
-    first moves the worst frame's surface by about 2 cm at 1.5 m).  Each
+    first moves the worst frame's surface by about 2 cm at 1.5 m), capped so
+    that no frame moves by more than `max_step` (|rho| + 1.5 |phi|, metres)
+    in one step, and a trial is accepted when L falls by at least `armijo`
+    times the decrease the gradient predicts.  Without the cap and the
+    sufficient-decrease test the doubling steps can carry the poses into
+    another basin of L (on the configured 1 deg / 5 mm jitter: loss 4e-6
+    with the rotation error at 0.76 deg, against 9e-7 and 0.08 deg).  Each
     trial is one forward; the accepted trial's forward is the one the adjoint
     runs on.  Returns a dict: R, t, losses (per step), forward_ms and
     adjoint_ms (CUDA events, per accepted step), forward_evaluations."""
@@ -307,16 +314,20 @@ def refine_poses(depth, R, t, D_model, W_model, cfg, steps=50, blocks_every=10, 
             lam = damping * torch.diagonal(H, dim1=1, dim2=2).mean(-1)
             Hd = H + (lam + 1e-30)[:, None, None] * torch.eye(6, dtype=H.dtype, device=H.device)
         d = -torch.linalg.solve(Hd, g)
+        move = max(float((d[:, :3].norm(dim=1) + 1.5 * d[:, 3:].norm(dim=1)).max()), 1e-30)
         if alpha is None:
-            alpha = 0.02 / max(float((d[:, :3].norm(dim=1) + 1.5 * d[:, 3:].norm(dim=1)).max()), 1e-30)
+            alpha = 0.02 / move
         else:
             alpha *= 2.0
+        if max_step is not None:
+            alpha = min(alpha, max_step / move)
+        slope = float((g * d).sum())   # dL/dalpha at alpha = 0 (negative: d is a descent direction)
         while True:
             R2, t2 = se3_left_update(R, t, (alpha * d).to(R.dtype))
             loss2, Rv, tv, e0, e1 = evaluate(R2, t2)
             out["forward_evaluations"] += 1
             L2 = float(loss2.item())
-            if L2 < L or alpha < 1e-12:
+            if L2 < L + armijo * alpha * min(slope, 0.0) or alpha < 1e-12:
                 break
             del loss2, Rv, tv
             alpha *= 0.5

@@ -211,6 +211,12 @@ class TSDFVolume:
     def reset(self, stream=None):
         L.check(self._lib.gbt_volume_reset(self._h, _stream_handle(stream)))
 
+    def check(self, stream=None):
+        """Synchronises and raises GbtError (GBT_ERR_TIMEOUT) if a kernel gave up
+        a bounded wait while working on this volume (its contents are then
+        undefined until reset); the mark is cleared."""
+        L.check(self._lib.gbt_volume_check(self._h, _stream_handle(stream)))
+
     # -- integrate -----------------------------------------------------------
     def integrate(self, color, depth, camera_pose, depth_scale=0.001, stream=None):
         """TSDFVolume::integrate(color, depth, pose) (tsdf_volume.cu:257-290).
@@ -234,7 +240,10 @@ class TSDFVolume:
         return True
 
     def integrate_frames(self, depths, poses, depth_scale=0.001, brick=0, ctas_per_sm=0, stream=None):
-        """Integrates up to 32 frames in one pass over the volume (frames applied in order)."""
+        """Integrates up to 32 frames in one pass over the volume (frames applied in order).
+        brick: the tile shape of gbt_integrate_tuned (0..7), or 8 for bricks
+        streamed into shared memory by the Tensor Memory Accelerator (passes
+        of up to 16 frames, x extent a multiple of 4); results are the same."""
         n = len(depths)
         arr = (L.Frame * n)()
         for i in range(n):

@@ -149,6 +149,13 @@ gbt_status gbt_volume_get_cfg(const gbt_volume* vol, gbt_volume_cfg* cfg);
  * (tsdf_volume.cuh:57-83). */
 gbt_status gbt_volume_get_info(const gbt_volume* vol, gbt_volume_info* info);
 
+/* Synchronises `stream` and reports whether a kernel that worked on the
+ * volume gave up a bounded device-side wait (GBT_ERR_TIMEOUT: the volume's
+ * contents are undefined until gbt_volume_reset or a load; the mark is
+ * cleared by this call).  No counterpart in the reference, whose kernels do
+ * not wait on the GPU. */
+gbt_status gbt_volume_check(gbt_volume* vol, void* stream);
+
 /* Replaces transformation_voxels_data (tsdf_volume.cuh:86-92).  The engine
  * never stores the per-voxel {float3 centre, float4 quaternion} records; the
  * first call materialises them (28 bytes per voxel, packed as in
@@ -165,7 +172,12 @@ gbt_status gbt_integrate(gbt_volume* vol, const gbt_frame* frames, int32_t nfram
 /* Same as gbt_integrate with an explicit tile shape and grid size, for the
  * autotuner.  brick: 0 = 32x4x4 voxels, 1 = 16x8x4, 2 = 32x2x8, 3 = 64x2x4;
  * 4..7 = the same shapes with each warp's depth samples staged in shared
- * memory frame by frame (passes of up to 16 frames; same results).
+ * memory frame by frame (passes of up to 16 frames; same results);
+ * 8 = bricks of 32x4x4 voxels whose distances and weights the Tensor Memory
+ * Accelerator copies into shared memory a few bricks ahead of the one being
+ * updated (passes of up to 16 frames, x extents that are multiples of 4;
+ * same results).  Its waits for those copies are bounded: one that gives up
+ * marks the volume (see gbt_volume_check).
  * ctas_per_sm: 0 = as many CTAs as the kernel keeps resident on an SM. */
 gbt_status gbt_integrate_tuned(gbt_volume* vol, const gbt_frame* frames, int32_t nframes, int32_t brick,
                                int32_t ctas_per_sm, void* stream);
@@ -408,12 +420,18 @@ const char* gbt_last_error(void);
  *   GBT_INJECT_LAUNCH_ERROR: leaves a launch error pending in the engine's
  *     CUDA runtime, as a caller's failed launch would: a kernel launched with
  *     a block of zero threads, which the runtime refuses on the host.
- *   GBT_INJECT_NONE: cancels pending allocation failures.
- * Nothing here touches the GPU or its memory. */
+ *   GBT_INJECT_HOLD_COPY: the next `count` streamed passes (brick 8 of
+ *     gbt_integrate_tuned) issue no copy for the first brick of their first
+ *     CTA, whose wait for it then gives up after about a second: the pass
+ *     ends early and marks the volume for gbt_volume_check.  No memory is
+ *     touched that a normal pass would not touch.
+ *   GBT_INJECT_NONE: cancels pending allocation failures and held copies.
+ * Nothing here faults the GPU. */
 enum {
     GBT_INJECT_NONE = 0,
     GBT_INJECT_ALLOC = 1,
-    GBT_INJECT_LAUNCH_ERROR = 2
+    GBT_INJECT_LAUNCH_ERROR = 2,
+    GBT_INJECT_HOLD_COPY = 3
 };
 gbt_status gbt_debug_inject(int32_t what, int64_t skip, int64_t count);
 

@@ -103,6 +103,9 @@ def test_null_arguments_are_rejected(engine_lib):
     cfg = L.VolumeCfg()
     assert lib.gbt_volume_get_cfg(None, C.byref(cfg)) == L.GBT_ERR_INVALID_ARG
     assert b"gbt_volume_get_cfg" in lib.gbt_last_error()
+    assert lib.gbt_volume_check(None, None) == L.GBT_ERR_INVALID_ARG
+    assert lib.gbt_debug_inject(L.INJECT_HOLD_COPY, 0, -1) == L.GBT_ERR_INVALID_ARG
+    assert lib.gbt_debug_inject(L.INJECT_NONE, 0, 0) == L.GBT_OK
     assert lib.gbt_volume_destroy(None) == L.GBT_OK
 
 
