@@ -1240,12 +1240,12 @@ def main():
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     # DRAM bytes and warp instructions: one ncu capture of the five
     # integrate_batch_kernel launches of a step of this workload (512^3, 300
-    # frames in windows of 64 and 44, brick 2, resident CTAs): 4.382 GB read +
-    # 3.176 GB written and 29.94 G warp instructions for the step (bricks no
+    # frames in windows of 64 and 44, brick 2, resident CTAs): 4.372 GB read +
+    # 3.176 GB written and 28.17 G warp instructions for the step (bricks no
     # frame sees are neither loaded nor stored).  Only for that launch shape;
     # other grids, shapes and the fixed mode were not captured.
     captured = (path == "batched" and args.mode == "compat" and args.grid == 512 and nf == 300 and K == 64)
-    traffic = (4.38248e9 + 3.17570e9) / n_passes if captured else None
+    traffic = (4.37171e9 + 3.17576e9) / n_passes if captured else None
     peak, peak_kind = peaks()
     # The kernel is bound by instruction issue, not by HBM (a window of K
     # frames shares each voxel's 16 bytes).  Its issue roofline: the captured
@@ -1254,7 +1254,7 @@ def main():
     # SM at the median SM clock sampled while timing.
     issue = None
     if captured:
-        warp_inst_per_update = 29.93774e9 / (512 ** 3 * 300)
+        warp_inst_per_update = 28.16625e9 / (512 ** 3 * 300)
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         sm_mhz = (clocks.summary().get("sm_mhz") or 0.0)
         upd_per_s = nvox * (nf / n_passes) / (launch_ms * 1e-3)
