@@ -1275,20 +1275,19 @@ __device__ __forceinline__ void mc_load_tables(unsigned char* s_count, unsigned 
 //     x corners; the x + 1 nibble is the next lane's.  Each row's triangle
 //     counts go to the words of the tiles (mc_tile_cubes(MODE) cubes in
 //     linear cube order, words starting at 0) its cubes fall in.
-// (2) mc_scan_kernel: one CTA per superblock of 1024 tiles turns the tile
-//     counts into exclusive offsets in place and lists the tiles that have
-//     triangles, from the superblock totals the count kernel kept; the last
-//     writes the total.
+// (2) mc_reduce_kernel: one CTA per superblock of 1024 tiles sums its tile
+//     counts (triangles, tiles with triangles); mc_scan_kernel: one CTA per
+//     superblock turns the tile counts into exclusive offsets in place and
+//     lists the tiles that have triangles, from those superblock totals; the
+//     last writes the total.
 // (3) mc_emit_kernel: CTAs take listed tiles by ticket, classify the tile
 //     again, scan its counts and write its triangles from the tile's offset.
 // Triangles come out in the reference's linear cube order.
-// Adds n > 0 triangles to tile t's word and to its superblock's totals (the
-// triangles, and the tiles whose word was 0 until now).
+// Adds n > 0 triangles to tile t's word.  (The superblock totals are summed
+// from the words afterwards, by mc_reduce_kernel: atomics on them from the
+// rows of every warp contend for a few addresses.)
 __device__ __forceinline__ void mc_add_tile(const McArgs& a, uint64_t t, unsigned n) {
-    const unsigned long long old = atomicAdd(a.status + t, (unsigned long long)n);
-    unsigned long long* sb = a.super + 2 * (t >> kMcSuperShift);
-    atomicAdd(sb, (unsigned long long)n);
-    if (old == 0ull) atomicAdd(sb + 1, 1ull);
+    atomicAdd(a.status + t, (unsigned long long)n);
 }
 
 constexpr uint32_t kMcSegCubes = 31;      // cubes per segment: 32 voxel columns
@@ -1591,6 +1590,31 @@ __global__ void __launch_bounds__(kMcThreads) mc_count4_kernel(const __grid_cons
 }
 
 constexpr int kMcScanThreads = 1 << kMcSuperShift;   // one thread per tile of a superblock
+
+// Superblock totals: one CTA per superblock of 1024 tiles sums its tile
+// counts into super[2 sb] (triangles) and super[2 sb + 1] (tiles with
+// triangles).
+__global__ void __launch_bounds__(kMcScanThreads) mc_reduce_kernel(const __grid_constant__ McArgs a) {
+    __shared__ unsigned long long s_part[kMcScanThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t t = (uint64_t)blockIdx.x * kMcScanThreads + tid;
+    const unsigned long long c = t < a.ntiles ? a.status[t] : 0ull;
+    // packed as the scan packs its sums: triangles << 24 | tiles with triangles
+    unsigned long long v = (c << 24) | (c != 0ull ? 1ull : 0ull);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long x = lane < kMcScanThreads / 32 ? s_part[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) {
+            a.super[2 * blockIdx.x] = x >> 24;
+            a.super[2 * blockIdx.x + 1] = x & 0xffffffull;
+        }
+    }
+}
 
 // Exclusive offsets of the tiles (in place), the list of tiles with
 // triangles, the triangle total and the list length.  One CTA per superblock
@@ -2230,7 +2254,9 @@ cudaError_t launch_mc_mode(const McArgs& a, cudaStream_t s) {
         mc_count4_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
     else
         mc_count_kernel<MODE><<<(int)grid, kMcThreads, 0, s>>>(a);
-    mc_scan_kernel<<<(unsigned)((a.ntiles + kMcScanThreads - 1) / kMcScanThreads), kMcScanThreads, 0, s>>>(a);
+    const unsigned nsuper = (unsigned)((a.ntiles + kMcScanThreads - 1) / kMcScanThreads);
+    mc_reduce_kernel<<<nsuper, kMcScanThreads, 0, s>>>(a);
+    mc_scan_kernel<<<nsuper, kMcScanThreads, 0, s>>>(a);
     grid = (long long)mg.sms * mg.per_emit;
     const long long tiles_per_cta = kMcThreads / 32;   // a warp per listed tile at least
     if (grid > ((long long)a.ntiles + tiles_per_cta - 1) / tiles_per_cta)
