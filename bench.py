@@ -653,12 +653,14 @@ def refine_workload(args, torch):
 
 def _refine_gn(args, torch, DF, dj, R, t, D0, W0, cfg, Dm, cmask, Wm, cam, tr, errors):
     """The refinement of cuphoto.diff.refine_poses: adjoint gradients, per-frame
-    6x6 Gauss-Newton preconditioning, backtracking line search."""
+    6x6 Gauss-Newton preconditioning, backtracking line search with the step
+    capped at 1 cm of motion and a sufficient-decrease test."""
     r = DF.refine_poses(dj, R, t, Dm, Wm, cfg, steps=args.refine_steps, D0=D0, W0=W0)
     after = errors(r["R"], r["t"])
     losses = r["losses"]
     extra = {"method": "adjoint gradient, per-frame 6x6 Gauss-Newton preconditioner (frame-to-model SDF), "
-                       "backtracking line search", "forward_evaluations": r["forward_evaluations"],
+                       "backtracking line search (steps capped at 1 cm of motion, sufficient decrease 1e-4)",
+             "forward_evaluations": r["forward_evaluations"],
              "steps": args.refine_steps, "loss_trace": losses[:: max(1, len(losses) // 10)]}
     return after, float(np.median(r["forward_ms"])), float(np.median(r["adjoint_ms"])), losses, extra
 
