@@ -842,7 +842,8 @@ __global__ void __launch_bounds__(128, LANE_BRICKS ? 10 : 0) integrate_kernel(co
 // four warps together), and a stream per warp over slabs of 32 x 4 x 1
 // voxels with the next slab's depth samples gathered before the current
 // slab's update took 0.356 ms (40 % more instructions in culling and copy
-// management per voxel).  It stays selectable for the autotuner.
+// management per voxel).  It stays selectable (brick 8), outside the
+// autotuner's default candidates.
 //
 // Waits are bounded: a stage whose copy does not arrive within about a second
 // sets kStatusWaitExpired in the volume's status word; the CTA then waits
