@@ -961,8 +961,8 @@ def multiscene(args, torch, rank, world, local):
         "per_scene": per_scene,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * float(np.mean(e2e))},
-        # per step: a reset per volume, the batched launches, three mesh launches per volume
-        "gpu_launches": args.steps * (4 * len(vols) + ((max(nfs) + fpl - 1) // fpl)),
+        # per step: a reset per volume, the batched launches, four mesh launches per volume
+        "gpu_launches": args.steps * (5 * len(vols) + ((max(nfs) + fpl - 1) // fpl)),
         "clocks": clocks.summary(),
         "autotune": {"candidates": len(table)},
     }
@@ -1362,8 +1362,8 @@ def main():
         "mesh": {"triangles_per_s": ntri / (float(np.mean(mesh_ms)) * 1e-3) if ntri else 0.0, "triangles": ntri},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": float(np.mean(e2e_ms))},
-        # per step: reset, the integrate launches, three mesh launches (count, scan, emit)
-        "gpu_launches": args.steps * (1 + n_passes + 3),
+        # per step: reset, the integrate launches, four mesh launches (count, reduce, scan, emit)
+        "gpu_launches": args.steps * (1 + n_passes + 4),
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
         "autotune": {"ns_per_update": tune["ns_per_update"], "candidates": candidates},

@@ -1267,7 +1267,7 @@ __device__ __forceinline__ void mc_load_tables(unsigned char* s_count, unsigned 
     if (s_ends && threadIdx.x < 12) s_ends[threadIdx.x] = GBT_MC_EDGE_ENDS[threadIdx.x];
 }
 
-// Marching cubes in three launches, none of which waits on another CTA.
+// Marching cubes in four launches, none of which waits on another CTA.
 // (1) mc_count_kernel: a warp takes a segment of kMcSegCubes cubes along x in
 //     one cube layer and walks kMcRowsPerTask rows along y.  Lane l holds
 //     voxel column x0 + l; per row it loads its voxels at (y+1, z) and
