@@ -59,13 +59,15 @@ def test_streamed_pass_ragged_grids_vs_oracle(gpu, oracle, grid):
 
 @pytest.mark.parametrize("ctas", [1, 2])
 def test_streamed_pass_many_bricks_per_cta(gpu, ctas):
-    """Few CTAs over a 384x256x256 volume: each CTA culls its bricks in several
-    rounds of 128 and its queue of live bricks wraps around (more than 256 per
-    CTA) while copies are in flight; the volume is that of brick 0."""
+    """Few CTAs over a 512x512x384 volume (196,608 bricks: 1293 per CTA at one
+    CTA per SM): each CTA culls its bricks in many rounds of 128, and the
+    indices of its 256-entry ring of queued bricks wrap around (more live
+    bricks per CTA than the ring holds) while copies are in flight; the
+    volume is that of brick 0."""
     seq, tc = circle_case(n=256, frames=4, physical=2.56)
-    tc.voxel_grid_size = (384, 256, 256)
-    tc.physical_size = (3.84, 2.56, 2.56)
-    tc.global_offset = (-1.92, -1.28, -1.28)
+    tc.voxel_grid_size = (512, 512, 384)
+    tc.physical_size = (5.12, 5.12, 3.84)
+    tc.global_offset = (-2.56, -2.56, -1.92)
     imgs = list(seq.depth_u16)
     ref = _volumes(gpu, tc, imgs, seq.poses, 1, 0)
     out = _volumes(gpu, tc, imgs, seq.poses, 1, STREAMED, ctas_per_sm=ctas)
