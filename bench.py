@@ -493,11 +493,12 @@ def refine_workload(args, torch):
     frames (jittered ones at their erroneous poses) into a grid^3 volume
     over the 2.56 m cube, then marching cubes; CUDA-event timed.  (2) The
     model: the same integrate of the other frames only.  (3) Refinement: for
-    `refine_steps` Adam steps on the jittered frames' se(3) left updates,
-    integrate them (differentiable, FP32, 8-frame recompute chunks) into a
-    fresh volume and minimise the frame-to-model loss
-    L = sum c W (D - D_model)^2 / sum c W, c = [W_model > 0], through the
-    autograd Function (forward + adjoint timed per step).  Reports the
+    `refine_steps` steps on the jittered frames' se(3) left updates
+    (Gauss-Newton-preconditioned adjoint gradients, or Adam with
+    --refine-method adam), integrate them (differentiable, FP32, 8-frame
+    recompute chunks) into a fresh volume and minimise the frame-to-model
+    loss L = sum c W (D - D_model)^2 / sum c W, c = [W_model > 0], through
+    the autograd Function (forward + adjoint timed per step).  Reports the
     rotation, camera-centre and surface-registration errors before and
     after, and the adjoint's cost against the forward."""
     import ctypes as C
@@ -1014,6 +1015,27 @@ def onepass_workload(args, torch):
             "streamed_over_gathered": best["streamed"]["ms_per_frame"] / best["gathered"]["ms_per_frame"]}
 
 
+def refine_summary(args, torch):
+    """The large pose-refinement configuration (1024^3 voxels of 0.25 cm,
+    1000 frames 1280x720, 50 Gauss-Newton-preconditioned steps on 64
+    jittered frames; `--workload refine` with its defaults) run inside the
+    default line and reduced to its figures.  A failure here is reported in
+    the object and leaves the rest of the line intact."""
+    import copy
+    a2 = copy.copy(args)
+    a2.grid, a2.frames, a2.refine_frames, a2.refine_steps, a2.refine_method = 1024, 1000, 64, 50, "gn"
+    try:
+        r = refine_workload(a2, torch)
+    except Exception as e:
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+    finally:
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    keep = ("workload", "plain_forward", "refine_step_ms", "loss", "pose_error_before", "pose_error_after",
+            "reduction")
+    return {k: r[k] for k in keep if k in r}
+
+
 def multiscene_summary(args, torch, local):
     """The multi-scene configuration (16 seeded scenes, 64^3..384^3, 10..120
     frames, one batched launch per window, autotuned, graph-captured) run
@@ -1340,6 +1362,7 @@ def main():
         extras["fixed_mode_mesh"] = fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas)
         extras["differentiable"] = differentiable_c3(torch)
         extras["multiscene"] = multiscene_summary(args, torch, local)
+        extras["refine"] = refine_summary(args, torch)
         cpu = cpu_baseline(args, cam, scene, poses)
     else:
         cpu = None
