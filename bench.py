@@ -1015,6 +1015,26 @@ def onepass_workload(args, torch):
             "streamed_over_gathered": best["streamed"]["ms_per_frame"] / best["gathered"]["ms_per_frame"]}
 
 
+def onepass_summary(args, torch):
+    """One frame per pass over the default workload's 512^3 volume (the
+    reference's calling pattern, one TSDFVolume::integrate per frame) inside
+    the default line: `--workload onepass` for every brick shape, the depth
+    gathered, staged in shared memory and the bricks streamed by tensor
+    copies.  A failure here is reported in the object and leaves the rest of
+    the line intact."""
+    import copy
+    a2 = copy.copy(args)
+    a2.mode = "compat"
+    try:
+        r = onepass_workload(a2, torch)
+    except Exception as e:
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+    finally:
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return r
+
+
 def refine_summary(args, torch):
     """The large pose-refinement configuration (1024^3 voxels of 0.25 cm,
     1000 frames 1280x720, 50 Gauss-Newton-preconditioned steps on 64
@@ -1362,6 +1382,7 @@ def main():
         extras["fixed_mode_mesh"] = fixed_mode_mesh(args, torch, cam, depths, poses, K, brick, ctas)
         extras["differentiable"] = differentiable_c3(torch)
         extras["multiscene"] = multiscene_summary(args, torch, local)
+        extras["one_frame_per_call"] = onepass_summary(args, torch)
         extras["refine"] = refine_summary(args, torch)
         cpu = cpu_baseline(args, cam, scene, poses)
     else:
