@@ -75,6 +75,24 @@ def test_streamed_pass_many_bricks_per_cta(gpu, ctas):
     _same(out, ref)
 
 
+@pytest.mark.parametrize("fmt", ["u16", "f32"])
+def test_streamed_pass_pitched_images(gpu, fmt):
+    """Depth images with 3 unused elements after each row (the samples are
+    read through the pitch): brick 8 = brick 0, bit for bit."""
+    from test_gpu_integrate import _pitched
+    seq, tc = circle_case(n=96, frames=8, max_weight=8)
+    imgs = list(seq.depth_u16) if fmt == "u16" else list(seq.depth_m())
+    dd = [_pitched(gpu, d, 3) for d in imgs]
+    out = {}
+    for brick in (0, STREAMED):
+        vol = TSDFVolume(tc)
+        vol.integrate_frames(dd, seq.poses, depth_scale=0.001, brick=brick)
+        gpu.cuda.synchronize()
+        out[brick] = (vol.voxel_distances_data().cpu().numpy(), vol.voxel_weights_data().cpu().numpy())
+    assert (out[0][1] > 0).mean() > 0.05
+    _same(out[STREAMED], out[0])
+
+
 def test_streamed_pass_rejects_what_it_cannot_run(gpu):
     seq, tc = frontal_case(77, 40, 32, frames=17)
     vol = TSDFVolume(tc)
